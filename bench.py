@@ -1,0 +1,317 @@
+"""Benchmark of the training hot path: one step = residual + boundary terms + loss + parameter
+gradient of every collocation point, then the Adam update.
+
+Workload (default): steady 2D Navier-Stokes, Kovasznay flow at Re=20, 'autograd' mode, MLP
+2->128x5->3 tanh, 1024x1024 = 1,048,576 collocation points plus 4 x 1024 Dirichlet points per
+output. Synthetic, seeded inputs: the grid and the closed-form boundary values are generated here;
+the network is seeded torch default init.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload kovasznay|burgers|kdv|heat] [--points-per-axis n]
+
+Our arm prints one JSON line with the device-resident throughput (value), the end-to-end
+throughput through the public API with host buffers (e2e), the roofline of the fused kernel, a
+CPU baseline (the oracle's restatement of the reference algorithm, timed on the host cores on a
+bounded sample), sampled GPU clocks and the number of library kernel launches. --impl reference
+times that CPU restatement alone on the same workload family.
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, 'tests'))
+
+METRIC = 'train steps/s & colloc pts/s, fused jet+adjoint vs plain path, 1 GB300, at tol'
+UNIT = 'colloc_pts/s'
+L2_BYTES = 129 * 1024 * 1024
+
+WORKLOADS = {
+    # name: (case builder name, kwargs at full size, kwargs of the CPU sample, description)
+    'kovasznay': ('kovasznay_ag', dict(n=1023), dict(n=63),
+                  'kovasznay_re20_autograd_2-128x5-3_1024x1024'),
+    'burgers': ('burgers_ag', dict(n=100), dict(n=100), 'burgers_autograd_2-32x4-1_101x101'),
+    'kdv': ('kdv_ag', dict(nx=255, nt=127), dict(nx=63, nt=31), 'kdv_autograd_2-64x4-1_256x128'),
+    'heat': ('heat_nn', dict(n=20), dict(n=20), 'heat_nn_2-100x3-1_21x21'),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default='kovasznay', choices=sorted(WORKLOADS))
+    ap.add_argument('--points-per-axis', type=int, default=None)
+    ap.add_argument('--precision', default='fp32')
+    ap.add_argument('--cpu-seconds', type=float, default=20.0)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    return ap.parse_args()
+
+
+def builder_for(name, kw):
+    import cases
+    fn = getattr(cases, WORKLOADS[name][0])
+    return lambda api, dtype='float32': fn(api, dtype=dtype, **kw)
+
+
+def full_kwargs(args):
+    kw = dict(WORKLOADS[args.workload][1])
+    if args.points_per_axis:
+        if 'n' in kw:
+            kw['n'] = args.points_per_axis - 1
+        else:
+            kw['nx'] = kw['nt'] = args.points_per_axis - 1
+    return kw
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(args, max_seconds):
+    """The oracle (fp32 restatement of the reference path: nested autograd.grad + double backward,
+    torch.optim.Adam) on the host cores, on a bounded sample of the workload."""
+    import torch
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    kw = WORKLOADS[args.workload][2]
+    prob, net = O.build_problem(builder_for(args.workload, kw), 'float32')
+    n_pts = prob.points.shape[0]
+    opt = torch.optim.Adam(net.parameters(), lr=1e-3)
+
+    def step():
+        opt.zero_grad()
+        r = prob.evaluate(net)
+        r['loss'].backward()
+        opt.step()
+    for _ in range(2):
+        step()
+    times = []
+    t_end = time.perf_counter() + max_seconds
+    while len(times) < 3 or (time.perf_counter() < t_end and len(times) < 200):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    sec = statistics.median(times)
+    return dict(value=n_pts / sec, unit=UNIT, cores=threads, kind='port',
+                sample=f'{WORKLOADS[args.workload][0]} {kw}: {n_pts} residual points, '
+                       f'{len(times)} Adam steps, median {sec * 1e3:.1f} ms/step, torch '
+                       f'{torch.__version__} fp32 on {threads} threads',
+                steps_per_s=1.0 / sec, points=n_pts)
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', f'--id={self.index}', f'--query-gpu={self.FIELDS}',
+                 '--format=csv,noheader,nounits', '-lms', '100'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in getattr(self, 'lines', []):
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ----------------------------------------------------------------------------- our arm
+def read_traffic(tag):
+    """DRAM bytes per collocation point of the fused kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, 'profiles', f'{tag}.txt')
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith('dram_bytes_per_point:'):
+            return float(ln.split(':')[1])
+    return None
+
+
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300 import _lib
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    kw = full_kwargs(args)
+    domain, bnd, eq, net, ckw = builder_for(args.workload, kw)(T)
+    ckw = dict(ckw)
+    model = T.Model(net, domain, eq, bnd)
+    model.compile(ckw.pop('mode'), precision=args.precision, **ckw)
+    sol = model.solution_cls
+    plan = sol.plan
+    n_pts = sol.ir.n_residual_rows
+    opt = T.Optimizer('Adam', {'lr': 1e-3}).optimizer_choice(model.mode, model.net)
+    flush = torch.empty(2 * L2_BYTES // 4, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def device_step():
+        plan.loss_grad(sol.flat, sol._grad, sol._loss_buf, sol._outputs)
+
+    # ---- device-resident throughput
+    for _ in range(args.warmup):
+        device_step()
+        opt.apply(sol._grad)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = _lib.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        for e0, e1, e2 in ev:
+            flush.zero_()                      # evict L2 between timed iterations
+            e0.record(stream)
+            device_step()
+            e1.record(stream)
+            opt.apply(sol._grad)
+            e2.record(stream)
+        torch.cuda.synchronize()
+    launches = _lib.launch_count() - launches0
+    step_ms = [a.elapsed_time(c) for a, _, c in ev]
+    kern_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t)
+    ms_per_step = total_ms / args.steps
+    value = world * n_pts / (ms_per_step / 1e3)
+
+    # ---- end to end through the public API with host buffers
+    pts_index = sol.ir.groups[sol.ir.residual_group].sites[0].points
+    dev_pts = plan.arrays[pts_index]
+    host_pts = dev_pts.cpu().pin_memory()
+    for _ in range(2):
+        dev_pts.copy_(host_pts, non_blocking=True)
+        opt.zero_grad()
+        loss, _ = sol.evaluate()
+        loss.backward()
+        opt.step()
+        loss.item()
+    torch.cuda.synchronize()
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        dev_pts.copy_(host_pts, non_blocking=True)
+        opt.zero_grad()
+        loss, _ = sol.evaluate()
+        loss.backward()
+        opt.step()
+        loss.item()
+    e2e_sec = (time.perf_counter() - t0) / e2e_steps
+    e2e = {'value': world * n_pts / e2e_sec, 'unit': UNIT,
+           'h2d_bytes_per_step': host_pts.numel() * 4, 'd2h_bytes_per_step': 4}
+
+    peaks_path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+    bf16 = peaks.get('bf16_tflops', 1900.0)
+    flops = plan.info.flops_hidden
+    kern_s = statistics.mean(kern_ms) / 1e3
+    achieved = flops / kern_s / 1e12
+    peak = bf16 / 2.0   # dense TF32 tensor rate = half the measured dense BF16 rate
+    tag = f'fused_fp32_{args.workload}'
+    tpp = read_traffic(tag)
+    roofline = {'bound': 'tensor', 'achieved': round(achieved, 3), 'peak': round(peak, 1),
+                'unit': 'TFLOP/s', 'frac': round(achieved / peak, 5),
+                'traffic': None if tpp is None else int(tpp * n_pts),
+                'kernel': 'tdg::fused_fp32_kernel (+ loss/gradient reductions)',
+                'kernel_ms': round(statistics.mean(kern_ms), 4),
+                'algorithmic_flops_per_launch': flops,
+                'peak_source': 'MEASURED_PEAKS.json bf16_tflops / 2 (dense TF32 = half of BF16)'
+                if peaks else 'fallback 1.9 PFLOP/s bf16 / 2'}
+    line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
+            'steps_per_s': round(1e3 / ms_per_step, 3), 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded grid, closed-form boundary data, seeded torch init)',
+            'config': {'workload': WORKLOADS[args.workload][3], 'collocation_points': n_pts,
+                       'params': plan.n_params, 'precision': args.precision, 'form': 'fused',
+                       'optimizer': 'Adam lr=1e-3',
+                       'l2': 'flushed between timed steps (256 MiB write)',
+                       'parallelism': f'replicas x{world}'},
+            'e2e': e2e, 'roofline': roofline, 'gpu_launches': int(launches),
+            'clocks': clk.summary(), 'impl': 'ours'}
+    return line
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        base = cpu_baseline(args, args.cpu_seconds)
+        print(json.dumps({'metric': METRIC, 'value': round(base['value'], 2), 'unit': UNIT,
+                          'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+                          'ms_per_step': round(1e3 / base['steps_per_s'], 3),
+                          'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+                          'dtype': 'f32', 'data': 'synthetic',
+                          'config': {'workload': WORKLOADS[args.workload][3],
+                                     'collocation_points': base['points']},
+                          'impl': 'reference',
+                          'cpu_baseline': {k: base[k] for k in ('value', 'unit', 'cores', 'kind',
+                                                                 'sample')},
+                          'e2e': {'value': round(base['value'], 2), 'unit': UNIT,
+                                  'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}))
+        return
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group('nccl')
+    line = run_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            line['cpu_baseline'] = {k: v for k, v in cpu_baseline(args, args.cpu_seconds).items()
+                                    if k in ('value', 'unit', 'cores', 'kind', 'sample')}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

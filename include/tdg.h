@@ -1,0 +1,213 @@
+/*
+ * tdg.h - C ABI of the GB300 training hot path for TEDEouS-style PINN problems.
+ *
+ * One call evaluates, for a tanh MLP, the residual of a differential operator and the boundary
+ * conditions at all collocation points, the weighted MSE loss, and the gradient of that loss with
+ * respect to every MLP parameter. The problem arrives as a flat, plain-old-data description
+ * (groups of points, evaluation sites, derivative streams and an operator program), so the same
+ * kernels serve the reference's 'NN' finite-difference mode and its 'autograd' mode.
+ *
+ * Reference interfaces these entry points replace (paths inside the TEDEouS project):
+ *   tdg_plan_create / tdg_plan_destroy
+ *       Solution.__init__ preparation: tedeous/solution.py:23-88 (Operator, Bounds, Losses built
+ *       once per compile); the derivative strategy chosen by Derivative.set_strategy
+ *       tedeous/derivative.py:347-363.
+ *   tdg_loss
+ *       Solution.evaluate(save_graph=False): tedeous/solution.py:129-168 -> Operator.operator_compute
+ *       tedeous/eval.py:223-232, Bounds.apply_bcs tedeous/eval.py:433-461,
+ *       Losses.compute tedeous/losses.py:230-263.
+ *   tdg_loss_grad
+ *       Solution.evaluate() followed by loss.backward() inside Closure._closure:
+ *       tedeous/optimizers/closure.py:49-64.
+ *   tdg_adam_step
+ *       the optimizer.step() of torch.optim.Adam selected by Optimizer.optimizer_choice:
+ *       tedeous/optimizers/optimizer.py:44-51.
+ *   tdg_dot_f64
+ *       the dot products of the L-BFGS two-loop recursion (torch.optim.LBFGS selected at
+ *       tedeous/optimizers/optimizer.py:50-51), computed in FP64.
+ *
+ * Conventions: every pointer passed to a compute entry point is a device pointer owned by the
+ * caller; nothing here frees caller memory. Calls are asynchronous on the given stream and never
+ * synchronise the host. A plan is not thread safe: use one plan per stream. Errors are returned
+ * as tdg_status codes and the message of the last failure on the calling thread is available
+ * from tdg_last_error(). No C++ exception crosses this boundary.
+ */
+#ifndef TDG_H_
+#define TDG_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDG_ABI_VERSION 1
+
+#define TDG_MAX_LAYERS 12      /* Linear layers of the MLP */
+#define TDG_MAX_DIN 4          /* input coordinates per point */
+#define TDG_MAX_DOUT 8         /* MLP outputs (dependent variables) */
+#define TDG_MAX_WIDTH 128      /* hidden width */
+#define TDG_MAX_ORDER 3        /* derivative order of one stream */
+#define TDG_MAX_STREAMS 16     /* (site, stream) pairs per row */
+#define TDG_MAX_SITES 16       /* evaluation sites per row */
+
+typedef enum {
+  TDG_OK = 0,
+  TDG_ERR_INVALID = 1,      /* malformed description or argument */
+  TDG_ERR_UNSUPPORTED = 2,  /* a feature outside what the kernels implement */
+  TDG_ERR_SHAPE = 3,        /* array sizes inconsistent with the description */
+  TDG_ERR_CUDA = 4,         /* a CUDA runtime call failed */
+  TDG_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+  TDG_ERR_NOMEM = 6         /* device allocation failed */
+} tdg_status;
+
+typedef enum {
+  TDG_PREC_FP32 = 0,        /* FP32 FMA hidden GEMMs (CUDA cores) */
+  TDG_PREC_TF32 = 1,        /* TF32 tensor-core hidden GEMMs, FP32 accumulate */
+  TDG_PREC_3XTF32 = 2,      /* split TF32 (hi*hi + hi*lo + lo*hi), FP32 accumulate */
+  TDG_PREC_BF16 = 3         /* BF16 tensor-core hidden GEMMs, FP32 accumulate */
+} tdg_precision;
+
+typedef enum {
+  TDG_FORM_FUSED = 0,       /* one persistent kernel: jet/stencil forward + operator + loss + adjoint */
+  TDG_FORM_PLAIN = 1        /* one launch per layer operation, activations kept in device memory */
+} tdg_form;
+
+/* tanh MLP: Linear(width[0]->width[1]), Tanh, ..., Linear(width[n-1]->width[n]). Parameters are one
+ * flat FP32 buffer in torch.nn.Module.parameters() order: W0 (width[1] x width[0], row-major), b0,
+ * W1, b1, ... */
+typedef struct {
+  int32_t n_layers;
+  int32_t width[TDG_MAX_LAYERS + 1];
+} tdg_mlp_desc;
+
+/* A derivative stream: d^order u / dx_axes[0] .. dx_axes[order-1]; order 0 is the value. */
+typedef struct {
+  int32_t order;
+  int32_t axes[TDG_MAX_ORDER];
+} tdg_stream_desc;
+
+/* An evaluation site: row i of the group is evaluated at points[i] + offset (FP32 add per axis,
+ * as the reference builds shifted grids), carrying n_streams derivative streams. */
+typedef struct {
+  int32_t points;            /* index into tdg_problem_desc.arrays: n_rows x d_in floats */
+  int32_t stream_first;      /* into tdg_problem_desc.streams */
+  int32_t n_streams;
+  float offset[TDG_MAX_DIN];
+} tdg_site_desc;
+
+/* part of a factor: weight * MLP_output[var] of stream `stream` at site `site` (indices relative
+ * to the group's first site and to that site's first stream). */
+typedef struct {
+  int32_t site;
+  int32_t stream;
+  float weight;
+} tdg_part_desc;
+
+/* factor of a term: (sum over its parts) ** power, reading MLP output `var`. */
+typedef struct {
+  int32_t part_first;
+  int32_t n_parts;
+  int32_t var;
+  float power;
+} tdg_factor_desc;
+
+/* term: coeff * product of factors, added to the group's output `output`. coeff_array >= 0 names a
+ * per-row coefficient array (n_rows floats) that replaces the scalar coeff. */
+typedef struct {
+  int32_t factor_first;
+  int32_t n_factors;
+  int32_t output;
+  int32_t coeff_array;
+  float coeff;
+} tdg_term_desc;
+
+/* a group of rows sharing one site/stream layout and one operator program. Output o of row i is
+ * compared with target[i * n_outputs + o] (0 when target_array < 0) and its squared error is
+ * added to loss slot slot_first + o. */
+typedef struct {
+  int32_t problem;           /* which parameter set (0 for a single solve) */
+  int32_t n_rows;
+  int32_t site_first, n_sites;
+  int32_t term_first, n_terms;
+  int32_t n_outputs;
+  int32_t slot_first;
+  int32_t target_array;
+  int64_t output_offset;     /* where rows' outputs go in the optional outputs buffer; -1: none */
+} tdg_group_desc;
+
+/* loss slot: loss += weight * sum(err^2); loss_normalized += weight_normalized * sum(err^2). */
+typedef struct {
+  int32_t problem;
+  double weight;
+  double weight_normalized;
+} tdg_slot_desc;
+
+typedef struct {
+  tdg_mlp_desc mlp;
+  int32_t n_problems;
+  int32_t n_groups;   const tdg_group_desc* groups;
+  int32_t n_sites;    const tdg_site_desc* sites;
+  int32_t n_streams;  const tdg_stream_desc* streams;
+  int32_t n_terms;    const tdg_term_desc* terms;
+  int32_t n_factors;  const tdg_factor_desc* factors;
+  int32_t n_parts;    const tdg_part_desc* parts;
+  int32_t n_slots;    const tdg_slot_desc* slots;
+  int32_t n_arrays;   const float* const* arrays;   /* device pointers */
+  const int64_t* array_len;                         /* element counts of arrays[] */
+  int32_t precision;  /* tdg_precision */
+  int32_t form;       /* tdg_form */
+} tdg_problem_desc;
+
+typedef struct {
+  int64_t n_params;           /* parameters of one problem */
+  int64_t workspace_bytes;    /* device memory owned by the plan */
+  int32_t n_tiles;
+  int32_t n_ctas;
+  int32_t n_segments;
+  int32_t max_streams;
+  double flops_hidden;        /* algorithmic hidden->hidden GEMM flops of one loss+gradient call */
+  double flops_total;         /* all layers, forward + backward */
+} tdg_plan_info;
+
+typedef struct {
+  float lr, beta1, beta2, eps, weight_decay;
+  int32_t maximize;
+} tdg_adam_desc;
+
+typedef struct tdg_plan tdg_plan;
+typedef struct CUstream_st* tdg_stream_t;   /* a cudaStream_t */
+
+int32_t tdg_abi_version(void);
+const char* tdg_last_error(void);
+int64_t tdg_launch_count(void);             /* kernels launched by this library so far */
+
+/* Validate the description, build tile schedules and device tables, allocate the workspace. */
+tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** plan);
+tdg_status tdg_plan_destroy(tdg_plan* plan);
+tdg_status tdg_plan_get_info(const tdg_plan* plan, tdg_plan_info* info);
+/* Replace the device pointer of array `index` (same length), e.g. freshly copied points. */
+tdg_status tdg_plan_set_array(tdg_plan* plan, int32_t index, const float* dev_ptr, int64_t n);
+
+/* loss[2*p] = loss, loss[2*p+1] = loss_normalized of problem p (device doubles). outputs, when
+ * not NULL, receives every group's per-row outputs at the groups' output_offset. */
+tdg_status tdg_loss(tdg_plan* plan, const float* params, double* loss, float* outputs,
+                    tdg_stream_t stream);
+/* As tdg_loss, and grad[p * n_params + j] = d loss_p / d params[p * n_params + j]. */
+tdg_status tdg_loss_grad(tdg_plan* plan, const float* params, float* grad, double* loss,
+                         float* outputs, tdg_stream_t stream);
+
+/* In-place Adam (torch.optim.Adam semantics, L2 weight_decay) on n floats; step is a device
+ * float counter incremented by the call, so the call can be replayed from a CUDA graph. */
+tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float* exp_avg_sq,
+                         float* step, int64_t n, const tdg_adam_desc* hp, tdg_stream_t stream);
+
+/* out[0] = sum_i a[i] * b[i] accumulated in FP64 (device double). */
+tdg_status tdg_dot_f64(const float* a, const float* b, int64_t n, double* out,
+                       tdg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TDG_H_ */

@@ -1,0 +1,185 @@
+"""Problem definitions shared by the golden generator, the oracle tests and the GPU parity tests.
+
+Each case is written once, in the reference's user-level format (``Domain.variable``,
+``Conditions.dirichlet/periodic``, ``Equation.add`` with term dicts), and is applied to any
+module set that exposes those names: the reference ``tedeous`` package (golden generation),
+this package (drop-in parity) or the oracle (CPU restatement).
+
+The workloads follow the benchmark definitions:
+  heat_nn      1D heat u_t = u_xx, 'NN' mode, 21x21 grid, MLP 2-100-100-100-1, lambda_bound=100,
+               h = grid step 1/20 (examples/examples_heat/example_heat_1d.py:147-151).
+  burgers_ag   Burgers u_t + u u_x = (0.01/pi) u_xx, 'autograd', 101x101, MLP 2-32x4-1
+               (examples/examples_burgers/example_Burgers_1d_paper.py:24-74).
+  kdv_ag       KdV u_t + 6 u u_x + u_xxx = 0, 'autograd', 256x128, MLP 2-64x4-1, IC 2 sech^2(x),
+               periodic u and u_x (examples/examples_korteweg_de_vries/example_KdV_periodic.py:94-160).
+  sweep_ag     u_t = a u_xx + b u u_x + c u on [0,1]^2, IC sin(pi x), zero Dirichlet, MLP 2-64x3-1.
+  kovasznay_ag steady 2D Navier-Stokes (Kovasznay flow, Re=20), outputs (u, v, p), MLP 2-128x5-3.
+"""
+
+import math
+
+import numpy as np
+import torch
+
+
+def mlp(widths, seed, dtype=torch.float32):
+    """tanh MLP as a torch.nn.Sequential of Linear/Tanh, seeded right before construction."""
+    torch.manual_seed(seed)
+    layers = []
+    for i in range(len(widths) - 1):
+        layers.append(torch.nn.Linear(widths[i], widths[i + 1]))
+        if i < len(widths) - 2:
+            layers.append(torch.nn.Tanh())
+    return torch.nn.Sequential(*layers).to(dtype)
+
+
+def heat_nn(api, n=20, seed=0, dtype='float32'):
+    domain = api.Domain()
+    domain.variable('x', [0, 1], n, dtype=dtype)
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [0, 1], 't': 0}, value=lambda g: torch.sin(np.pi * g[:, 0]))
+    bnd.dirichlet({'x': 0, 't': [0, 1]}, value=0)
+    bnd.dirichlet({'x': 1, 't': [0, 1]}, value=0)
+    eq = api.Equation()
+    eq.add({'du/dt': {'coeff': 1, 'du/dt': [1], 'pow': 1},
+            '-d2u/dx2': {'coeff': -1, 'd2u/dx2': [0, 0], 'pow': 1}})
+    net = mlp([2, 100, 100, 100, 1], seed)
+    compile_kw = dict(mode='NN', lambda_operator=1, lambda_bound=100, h=1.0 / n)
+    return domain, bnd, eq, net, compile_kw
+
+
+def burgers_ag(api, n=100, seed=0, dtype='float32', widths=(2, 32, 32, 32, 32, 1)):
+    mu = 0.01 / np.pi
+    domain = api.Domain()
+    domain.variable('x', [-1, 1], n, dtype=dtype)
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [-1, 1], 't': 0}, value=lambda g: -torch.sin(np.pi * g[:, 0]))
+    bnd.dirichlet({'x': -1, 't': [0, 1]}, value=0)
+    bnd.dirichlet({'x': 1, 't': [0, 1]}, value=0)
+    eq = api.Equation()
+    eq.add({'du/dt**1': {'coeff': 1., 'du/dt': [1], 'pow': 1, 'var': 0},
+            '+u*du/dx': {'coeff': 1, 'u*du/dx': [[None], [0]], 'pow': [1, 1], 'var': [0, 0]},
+            '-mu*d2u/dx2': {'coeff': -mu, 'd2u/dx2': [0, 0], 'pow': 1, 'var': 0}})
+    net = mlp(list(widths), seed)
+    compile_kw = dict(mode='autograd', lambda_operator=1, lambda_bound=1)
+    return domain, bnd, eq, net, compile_kw
+
+
+def burgers_nn(api, n=100, seed=0, dtype='float32'):
+    domain, bnd, eq, net, kw = burgers_ag(api, n=n, seed=seed, dtype=dtype)
+    kw = dict(mode='NN', lambda_operator=1, lambda_bound=1, h=2.0 / n)
+    return domain, bnd, eq, net, kw
+
+
+def kdv_ag(api, nx=255, nt=127, seed=0, dtype='float32', widths=(2, 64, 64, 64, 64, 1)):
+    domain = api.Domain()
+    domain.variable('x', [-10, 10], nx, dtype=dtype)
+    domain.variable('t', [0, 1], nt, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [-10, 10], 't': 0}, value=lambda g: 2.0 / torch.cosh(g[:, 0]) ** 2)
+    bnd.periodic([{'x': -10, 't': [0, 1]}, {'x': 10, 't': [0, 1]}])
+    bnd.periodic([{'x': -10, 't': [0, 1]}, {'x': 10, 't': [0, 1]}],
+                 operator={'du/dx': {'coeff': 1, 'du/dx': [0], 'pow': 1, 'var': 0}})
+    eq = api.Equation()
+    eq.add({'1*du/dt**1': {'coeff': 1, 'du/dt': [1], 'pow': 1, 'var': 0},
+            '6*u**1*du/dx**1': {'coeff': 6, 'u*du/dx': [[None], [0]], 'pow': [1, 1], 'var': [0, 0]},
+            'd3u/dx3**1': {'coeff': 1, 'd3u/dx3': [0, 0, 0], 'pow': 1, 'var': 0}})
+    net = mlp(list(widths), seed)
+    compile_kw = dict(mode='autograd', lambda_operator=1, lambda_bound=10)
+    return domain, bnd, eq, net, compile_kw
+
+
+def sweep_params(n_solves=256, seed=0):
+    """Coefficients and grid sizes of the equation-discovery sweep (one row per solve)."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(0.01, 1.0, n_solves)
+    b = rng.uniform(-1.0, 1.0, n_solves)
+    c = rng.uniform(-0.5, 0.5, n_solves)
+    nx = rng.integers(16, 129, n_solves)
+    nt = rng.integers(16, 129, n_solves)
+    return [dict(a=float(a[i]), b=float(b[i]), c=float(c[i]), nx=int(nx[i]), nt=int(nt[i]))
+            for i in range(n_solves)]
+
+
+def sweep_ag(api, a=0.5, b=0.3, c=-0.2, nx=24, nt=20, seed=1000, dtype='float32',
+             widths=(2, 64, 64, 64, 1)):
+    """u_t - a u_xx - b u u_x - c u = 0 on its own nx x nt grid (nx, nt node counts)."""
+    domain = api.Domain()
+    domain.variable('x', [0, 1], nx - 1, dtype=dtype)
+    domain.variable('t', [0, 1], nt - 1, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [0, 1], 't': 0}, value=lambda g: torch.sin(np.pi * g[:, 0]))
+    bnd.dirichlet({'x': 0, 't': [0, 1]}, value=0)
+    bnd.dirichlet({'x': 1, 't': [0, 1]}, value=0)
+    eq = api.Equation()
+    eq.add({'du/dt': {'coeff': 1, 'du/dt': [1], 'pow': 1, 'var': 0},
+            '-a*d2u/dx2': {'coeff': -a, 'd2u/dx2': [0, 0], 'pow': 1, 'var': 0},
+            '-b*u*du/dx': {'coeff': -b, 'u*du/dx': [[None], [0]], 'pow': [1, 1], 'var': [0, 0]},
+            '-c*u': {'coeff': -c, 'u': [None], 'pow': 1, 'var': 0}})
+    net = mlp(list(widths), seed)
+    compile_kw = dict(mode='autograd', lambda_operator=1, lambda_bound=1)
+    return domain, bnd, eq, net, compile_kw
+
+
+KOV_RE = 20.0
+
+
+def kovasznay_exact(g):
+    """Closed-form Kovasznay flow (u, v, p) at points g[:, 0] = x, g[:, 1] = y."""
+    re = KOV_RE
+    lam = re / 2 - math.sqrt(re * re / 4 + 4 * math.pi ** 2)
+    x, y = g[:, 0], g[:, 1]
+    u = 1 - torch.exp(lam * x) * torch.cos(2 * math.pi * y)
+    v = lam / (2 * math.pi) * torch.exp(lam * x) * torch.sin(2 * math.pi * y)
+    p = 0.5 * (1 - torch.exp(2 * lam * x))
+    return u, v, p
+
+
+def kovasznay_ag(api, n=1023, seed=0, dtype='float32', widths=(2, 128, 128, 128, 128, 128, 3)):
+    """Kovasznay flow on an (n+1)^2 grid over [-0.5, 1] x [-0.5, 1.5]; Dirichlet (u, v, p) on 4 sides."""
+    nu = 1.0 / KOV_RE
+    domain = api.Domain()
+    domain.variable('x', [-0.5, 1.0], n, dtype=dtype)
+    domain.variable('y', [-0.5, 1.5], n, dtype=dtype)
+    bnd = api.Conditions()
+    sides = [{'x': -0.5, 'y': [-0.5, 1.5]}, {'x': 1.0, 'y': [-0.5, 1.5]},
+             {'x': [-0.5, 1.0], 'y': -0.5}, {'x': [-0.5, 1.0], 'y': 1.5}]
+    for side in sides:
+        for var in range(3):
+            bnd.dirichlet(dict(side), value=(lambda g, k=var: kovasznay_exact(g)[k]), var=var)
+    eq = api.Equation()
+    continuity = {
+        'du/dx': {'coeff': 1, 'du/dx': [0], 'pow': 1, 'var': 0},
+        'dv/dy': {'coeff': 1, 'dv/dy': [1], 'pow': 1, 'var': 1}}
+    mom_x = {
+        'u*du/dx': {'coeff': 1, 'u*du/dx': [[None], [0]], 'pow': [1, 1], 'var': [0, 0]},
+        'v*du/dy': {'coeff': 1, 'v*du/dy': [[None], [1]], 'pow': [1, 1], 'var': [1, 0]},
+        'dp/dx': {'coeff': 1, 'dp/dx': [0], 'pow': 1, 'var': 2},
+        '-nu*d2u/dx2': {'coeff': -nu, 'd2u/dx2': [0, 0], 'pow': 1, 'var': 0},
+        '-nu*d2u/dy2': {'coeff': -nu, 'd2u/dy2': [1, 1], 'pow': 1, 'var': 0}}
+    mom_y = {
+        'u*dv/dx': {'coeff': 1, 'u*dv/dx': [[None], [0]], 'pow': [1, 1], 'var': [0, 1]},
+        'v*dv/dy': {'coeff': 1, 'v*dv/dy': [[None], [1]], 'pow': [1, 1], 'var': [1, 1]},
+        'dp/dy': {'coeff': 1, 'dp/dy': [1], 'pow': 1, 'var': 2},
+        '-nu*d2v/dx2': {'coeff': -nu, 'd2v/dx2': [0, 0], 'pow': 1, 'var': 1},
+        '-nu*d2v/dy2': {'coeff': -nu, 'd2v/dy2': [1, 1], 'pow': 1, 'var': 1}}
+    eq.add(continuity)
+    eq.add(mom_x)
+    eq.add(mom_y)
+    net = mlp(list(widths), seed)
+    compile_kw = dict(mode='autograd', lambda_operator=1, lambda_bound=1)
+    return domain, bnd, eq, net, compile_kw
+
+
+# Small variants used for committed golden fixtures (full sizes where the reference finishes
+# in seconds on CPU).
+GOLDEN_CASES = {
+    'heat_nn': lambda api, dtype='float32': heat_nn(api, dtype=dtype),
+    'burgers_ag': lambda api, dtype='float32': burgers_ag(api, dtype=dtype),
+    'burgers_nn': lambda api, dtype='float32': burgers_nn(api, n=40, dtype=dtype),
+    'kdv_ag': lambda api, dtype='float32': kdv_ag(api, dtype=dtype),
+    'sweep_ag': lambda api, dtype='float32': sweep_ag(api, dtype=dtype),
+    'kovasznay_ag': lambda api, dtype='float32': kovasznay_ag(api, n=31, dtype=dtype),
+}

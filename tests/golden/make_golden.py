@@ -1,0 +1,112 @@
+"""Generate golden fixtures by running the reference TEDEouS package itself on CPU.
+
+Usage (needs the reference source tree; run from the repository root):
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+
+For each case in tests/cases.py GOLDEN_CASES this writes tests/golden/<case>.npz holding
+  weights      the seeded initial parameters (fp32, flattened in net.parameters() order)
+  loss32/64    loss from Solution.evaluate() of an fp32 and of an fp64 run of the same weights
+  lossn32/64   loss_normalized of the same evaluate() call
+  grad32/64    the flattened parameter gradient after loss.backward()
+  op64         the first rows of the residual field (fp64) and op_sumsq64 = sum(op^2) per column
+  bval64, true_bval64   boundary value matrices (fp64, padded per the reference)
+  curve32      loss values seen by the closure over 5 Adam(lr=1e-3) steps of Model.train(6)
+  final32      parameters after those 5 steps
+The reference needs one stub: SALib (imported by tedeous/callbacks/adaptive_lambda.py:4) is
+absent, so an empty module is installed in sys.modules before the import.
+"""
+
+import os
+import sys
+import types
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def load_reference(path):
+    stub = types.ModuleType('SALib')
+    stub.ProblemSpec = object
+    sys.modules['SALib'] = stub
+    sys.path.insert(0, path)
+    import tedeous.data as data
+    import tedeous.model as model
+    import tedeous.optimizers.optimizer as optimizer
+    import tedeous.callbacks.callback as callback
+    from tedeous.device import solver_device
+    solver_device('cpu')
+    api = types.SimpleNamespace(Domain=data.Domain, Conditions=data.Conditions,
+                                Equation=data.Equation, Model=model.Model,
+                                Optimizer=optimizer.Optimizer, Callback=callback.Callback)
+    return api
+
+
+def flat(tensors):
+    return torch.cat([t.detach().reshape(-1).to(torch.float64) for t in tensors]).numpy()
+
+
+def run_case(api, builder, dtype):
+    domain, bnd, eq, net, kw = builder(api, dtype=dtype)
+    w0 = flat(net.parameters()).astype(np.float32)
+    m = api.Model(net, domain, eq, bnd)
+    mode = kw.pop('mode')
+    m.compile(mode, **kw)
+    s = m.solution_cls
+    loss, lossn = s.evaluate()
+    loss.backward()
+    grad = flat(p.grad for p in m.solution_cls.model.parameters())
+    return dict(w0=w0, loss=float(loss.detach().reshape(-1)[0]),
+                lossn=float(lossn.detach().reshape(-1)[0]), grad=grad,
+                op=s.op.detach().to(torch.float64).numpy(),
+                bval=s.bval.detach().to(torch.float64).numpy(),
+                true_bval=s.true_bval.detach().to(torch.float64).numpy(),
+                bval_keys=list(s.bval_keys), bval_length=list(s.bval_length))
+
+
+def run_curve(api, builder, steps=5):
+    domain, bnd, eq, net, kw = builder(api, dtype='float32')
+    m = api.Model(net, domain, eq, bnd)
+    mode = kw.pop('mode')
+    m.compile(mode, **kw)
+    seen = []
+
+    class Record(api.Callback):
+        def on_epoch_end(self, logs=None):
+            seen.append(float(self.model.cur_loss.detach().reshape(-1)[0]))
+
+    m.train(api.Optimizer('Adam', {'lr': 1e-3}), steps + 1, callbacks=[Record()])
+    return np.array(seen), flat(m.net.parameters()).astype(np.float32)
+
+
+def main(ref_path):
+    import cases
+    api = load_reference(ref_path)
+    torch.set_num_threads(min(8, os.cpu_count() or 1))
+    only = sys.argv[2:] or list(cases.GOLDEN_CASES)
+    for name in only:
+        builder = cases.GOLDEN_CASES[name]
+        r32 = run_case(api, builder, 'float32')
+        r64 = run_case(api, builder, 'float64')
+        assert np.array_equal(r32['w0'], r64['w0'])
+        curve, final = run_curve(api, builder)
+        op = r64['op']
+        out = dict(weights=r32['w0'],
+                   loss32=r32['loss'], loss64=r64['loss'],
+                   lossn32=r32['lossn'], lossn64=r64['lossn'],
+                   grad32=r32['grad'].astype(np.float32), grad64=r64['grad'],
+                   op64=op[:2048], op_sumsq64=(op ** 2).sum(0), n_op=op.shape[0],
+                   bval64=r64['bval'], true_bval64=r64['true_bval'],
+                   bval_keys=np.array(r64['bval_keys']), bval_length=np.array(r64['bval_length']),
+                   curve32=curve, final32=final)
+        np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+        rel_l = abs(r32['loss'] - r64['loss']) / abs(r64['loss'])
+        rel_g = np.linalg.norm(r32['grad'] - r64['grad']) / np.linalg.norm(r64['grad'])
+        print(f'{name}: loss64={r64["loss"]:.9g} rel32={rel_l:.2e} grad rel32={rel_g:.2e} '
+              f'n_op={op.shape[0]} keys={r64["bval_keys"]} curve={curve}')
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')

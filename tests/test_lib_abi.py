@@ -1,0 +1,44 @@
+"""The C-ABI library loads on a machine without a GPU and exports every symbol of include/tdg.h;
+argument validation reports errors through status codes (no compute calls)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, 'include', 'tdg.h')).read()
+    return sorted(set(re.findall(r'^\w[\w\s\*]*?\b(tdg_\w+)\s*\(', src, re.M)))
+
+
+def test_header_and_binding_agree():
+    from torch_de_solver_gb300 import _lib
+    assert set(declared_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_library_exports_every_declared_symbol():
+    from torch_de_solver_gb300 import _lib
+    lib = _lib.load()
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    assert lib.tdg_abi_version() == 1
+
+
+def test_struct_sizes_match_header():
+    from torch_de_solver_gb300 import _lib
+    assert ctypes.sizeof(_lib.GroupDesc) == 48
+    assert ctypes.sizeof(_lib.SiteDesc) == 28
+    assert ctypes.sizeof(_lib.SlotDesc) == 24
+
+
+def test_invalid_arguments_return_status():
+    from torch_de_solver_gb300 import _lib
+    lib = _lib.load()
+    assert lib.tdg_plan_create(None, None) == _lib.ERR_INVALID
+    assert b'null' in lib.tdg_last_error()
+    assert lib.tdg_adam_step(None, None, None, None, None, 0, None, None) == _lib.ERR_INVALID
+    assert lib.tdg_dot_f64(None, None, 0, None, None) == _lib.ERR_INVALID
+    assert lib.tdg_plan_destroy(None) == _lib.OK

@@ -1,0 +1,16 @@
+"""GB300-native training hot path for TEDEouS-style physics-informed neural networks.
+
+Drop-in names: Domain, Conditions, Equation (tedeous.data), Model (tedeous.model), Optimizer
+(tedeous.optimizers.optimizer), Callback, solver_device. The per-step loss, residual, boundary
+terms and parameter gradient run in hand-written sm_103a CUDA kernels (libtdg.so, include/tdg.h).
+"""
+from .data import Conditions, Domain, Equation
+from .device import check_device, device_type, solver_device
+from .callbacks import Callback, CallbackList
+from .optimizer import FusedAdam, Optimizer
+from .solution import DevicePlan, Solution
+from .model import Model
+
+__all__ = ['Domain', 'Conditions', 'Equation', 'Model', 'Optimizer', 'FusedAdam', 'Solution',
+           'DevicePlan', 'Callback', 'CallbackList', 'solver_device', 'check_device',
+           'device_type']

@@ -1,0 +1,139 @@
+"""ctypes binding of libtdg.so, the C ABI declared in include/tdg.h.
+
+The library is built in-tree (torch_de_solver_gb300/libtdg.so) by csrc/build.py. There is no
+fallback: every compute call goes through this library, and importing it without the built
+library raises.
+"""
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'libtdg.so')
+
+MAX_LAYERS = 12
+MAX_DIN = 4
+MAX_DOUT = 8
+MAX_WIDTH = 128
+MAX_ORDER = 3
+MAX_STREAMS = 16
+MAX_SITES = 16
+
+OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_SHAPE, ERR_CUDA, ERR_TIMEOUT, ERR_NOMEM = range(7)
+PREC = {'fp32': 0, 'tf32': 1, '3xtf32': 2, 'bf16': 3}
+FORM = {'fused': 0, 'plain': 1}
+
+i32, i64, f32, f64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_double
+vp = ctypes.c_void_p
+
+
+class MlpDesc(ctypes.Structure):
+    _fields_ = [('n_layers', i32), ('width', i32 * (MAX_LAYERS + 1))]
+
+
+class StreamDesc(ctypes.Structure):
+    _fields_ = [('order', i32), ('axes', i32 * MAX_ORDER)]
+
+
+class SiteDesc(ctypes.Structure):
+    _fields_ = [('points', i32), ('stream_first', i32), ('n_streams', i32), ('offset', f32 * MAX_DIN)]
+
+
+class PartDesc(ctypes.Structure):
+    _fields_ = [('site', i32), ('stream', i32), ('weight', f32)]
+
+
+class FactorDesc(ctypes.Structure):
+    _fields_ = [('part_first', i32), ('n_parts', i32), ('var', i32), ('power', f32)]
+
+
+class TermDesc(ctypes.Structure):
+    _fields_ = [('factor_first', i32), ('n_factors', i32), ('output', i32), ('coeff_array', i32),
+                ('coeff', f32)]
+
+
+class GroupDesc(ctypes.Structure):
+    _fields_ = [('problem', i32), ('n_rows', i32), ('site_first', i32), ('n_sites', i32),
+                ('term_first', i32), ('n_terms', i32), ('n_outputs', i32), ('slot_first', i32),
+                ('target_array', i32), ('output_offset', i64)]
+
+
+class SlotDesc(ctypes.Structure):
+    _fields_ = [('problem', i32), ('weight', f64), ('weight_normalized', f64)]
+
+
+class ProblemDesc(ctypes.Structure):
+    _fields_ = [('mlp', MlpDesc), ('n_problems', i32),
+                ('n_groups', i32), ('groups', ctypes.POINTER(GroupDesc)),
+                ('n_sites', i32), ('sites', ctypes.POINTER(SiteDesc)),
+                ('n_streams', i32), ('streams', ctypes.POINTER(StreamDesc)),
+                ('n_terms', i32), ('terms', ctypes.POINTER(TermDesc)),
+                ('n_factors', i32), ('factors', ctypes.POINTER(FactorDesc)),
+                ('n_parts', i32), ('parts', ctypes.POINTER(PartDesc)),
+                ('n_slots', i32), ('slots', ctypes.POINTER(SlotDesc)),
+                ('n_arrays', i32), ('arrays', ctypes.POINTER(vp)), ('array_len', ctypes.POINTER(i64)),
+                ('precision', i32), ('form', i32)]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [('n_params', i64), ('workspace_bytes', i64), ('n_tiles', i32), ('n_ctas', i32),
+                ('n_segments', i32), ('max_streams', i32), ('flops_hidden', f64),
+                ('flops_total', f64)]
+
+
+class AdamDesc(ctypes.Structure):
+    _fields_ = [('lr', f32), ('beta1', f32), ('beta2', f32), ('eps', f32), ('weight_decay', f32),
+                ('maximize', i32)]
+
+
+# entry point -> (restype, argtypes); kept in step with include/tdg.h
+SIGNATURES = {
+    'tdg_abi_version': (i32, []),
+    'tdg_last_error': (ctypes.c_char_p, []),
+    'tdg_launch_count': (i64, []),
+    'tdg_plan_create': (i32, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(vp)]),
+    'tdg_plan_destroy': (i32, [vp]),
+    'tdg_plan_get_info': (i32, [vp, ctypes.POINTER(PlanInfo)]),
+    'tdg_plan_set_array': (i32, [vp, i32, vp, i64]),
+    'tdg_loss': (i32, [vp, vp, vp, vp, vp]),
+    'tdg_loss_grad': (i32, [vp, vp, vp, vp, vp, vp]),
+    'tdg_adam_step': (i32, [vp, vp, vp, vp, vp, i64, ctypes.POINTER(AdamDesc), vp]),
+    'tdg_dot_f64': (i32, [vp, vp, i64, vp, vp]),
+}
+
+_lib = None
+
+
+class TdgError(RuntimeError):
+    pass
+
+
+def load():
+    """Load libtdg.so once; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f'{LIB_PATH} is missing: build it with '
+                          f'`python -m torch_de_solver_gb300.csrc.build` (no CPU fallback exists)')
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.tdg_abi_version() != 1:
+        raise ImportError('libtdg.so ABI version mismatch')
+    _lib = lib
+    return lib
+
+
+def check(status, what):
+    if status != OK:
+        msg = load().tdg_last_error().decode(errors='replace')
+        if status == ERR_UNSUPPORTED:
+            raise NotImplementedError(f'{what}: {msg}')
+        raise TdgError(f'{what} failed (status {status}): {msg}')
+
+
+def launch_count():
+    return int(load().tdg_launch_count())

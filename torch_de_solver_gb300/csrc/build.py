@@ -1,0 +1,60 @@
+"""Build libtdg.so (the C-ABI CUDA library) in-tree with nvcc for sm_103a.
+
+Each translation unit compiles in parallel; the shared library links against the CUDA runtime.
+Usage: python -m torch_de_solver_gb300.csrc.build  (or build() from Python).
+"""
+import concurrent.futures
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+ROOT = os.path.dirname(PKG)
+SOURCES = ['tdg_plan.cu', 'tdg_fused.cu', 'tdg_util.cu']
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+LIB = os.path.join(PKG, 'libtdg.so')
+
+
+def nvcc():
+    for cand in (os.environ.get('NVCC'), shutil.which('nvcc'), '/usr/local/cuda/bin/nvcc'):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError('nvcc not found: set NVCC or put the CUDA toolkit on PATH')
+
+
+def build(verbose=False, extra=()):
+    obj_dir = os.path.join(PKG, '_build')
+    os.makedirs(obj_dir, exist_ok=True)
+    flags = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-I' + os.path.join(ROOT, 'include'),
+             '--expt-relaxed-constexpr', *ARCH, *extra]
+    if verbose:
+        flags += ['-Xptxas', '-v']
+    cc = nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(obj_dir, src.replace('.cu', '.o'))
+        cmd = [cc, *flags, '-c', os.path.join(HERE, src), '-o', obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f'nvcc failed for {src}:\n{r.stdout}\n{r.stderr}')
+        return obj, r.stderr
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        results = list(ex.map(compile_one, SOURCES))
+    if verbose:
+        for _, log in results:
+            sys.stderr.write(log)
+    objs = [o for o, _ in results]
+    tmp = LIB + '.tmp'
+    cmd = [cc, '-shared', *ARCH, '-o', tmp, *objs, '-cudart', 'shared']
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f'link failed:\n{r.stdout}\n{r.stderr}')
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == '__main__':
+    print(build(verbose='-v' in sys.argv))

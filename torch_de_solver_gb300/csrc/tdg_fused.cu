@@ -1,0 +1,566 @@
+// Fused FP32 training-step kernel: one persistent CTA per SM walks a contiguous range of tiles.
+// For each tile of (point, stream) rows it runs
+//   input layer -> [hidden GEMM -> tanh jet] x (L-2) -> output layer        (forward, Taylor mode)
+//   operator program (coefficient x product of derivative factors) -> squared error -> loss slot
+//   adjoint of the program -> output layer -> [tanh jet adjoint -> dW, dX GEMMs] ... -> input layer
+// The residual of the reference's 'autograd' mode (nested autograd.grad, tedeous/derivative.py:74-132)
+// is carried as derivative streams through each layer; its 'NN' mode (tedeous/derivative.py:30-58)
+// is carried as value streams at shifted sites. Loss (tedeous/losses.py:84-135) is reduced per CTA
+// in FP64; parameter gradients are written to per-CTA segments and reduced by a second kernel, so
+// the result is deterministic.
+#include "tdg_internal.h"
+
+namespace tdg {
+
+namespace {
+
+__device__ __forceinline__ float sig_k(int k, float t, float s1, float s2, float s3, float s4) {
+  // derivatives of tanh as functions of t = tanh(z): s1 = 1 - t^2, s2 = -2 t s1,
+  // s3 = s1 (6 t^2 - 2), s4 = t s1 (16 - 24 t^2)
+  return k == 0 ? t : k == 1 ? s1 : k == 2 ? s2 : k == 3 ? s3 : s4;
+}
+
+__device__ __forceinline__ float pow_f(float x, float p) {
+  if (p == 1.f) return x;
+  if (p == 2.f) return x * x;
+  if (p == 0.f) return 1.f;
+  if (p == 3.f) return x * x * x;
+  return powf(x, p);
+}
+
+__device__ __forceinline__ float dpow_f(float x, float p) {  // d/dx x^p
+  if (p == 1.f) return 1.f;
+  if (p == 2.f) return 2.f * x;
+  if (p == 0.f) return 0.f;
+  if (p == 3.f) return 3.f * x * x;
+  return p * powf(x, p - 1.f);
+}
+
+// Z[r][n] = sum_k H[r][k] W[n][k] (+ b[n] on value streams). 16x16 threads, 8x8 outputs each.
+__device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ W,
+                         float* __restrict__ Z, const float* __restrict__ bias,
+                         const DevGroup& G, int R, int N, int K) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  for (int k = 0; k < K; k += 4) {
+    float4 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = ty + 16 * i;
+      a[i] = r < R ? *reinterpret_cast<const float4*>(&H[r * LDS + k]) : make_float4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = tx + 16 * j;
+      if (n < N) {
+        const float4 b = *reinterpret_cast<const float4*>(&W[n * LDS + k]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          float v = acc[i][j];
+          v = fmaf(a[i].x, b.x, v);
+          v = fmaf(a[i].y, b.y, v);
+          v = fmaf(a[i].z, b.z, v);
+          v = fmaf(a[i].w, b.w, v);
+          acc[i][j] = v;
+        }
+      }
+    }
+  }
+  const int T = G.T;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = ty + 16 * i;
+    if (r >= R) continue;
+    const bool val = G.st_order[r / T] == 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = tx + 16 * j;
+      if (n < N) Z[r * LDS + n] = acc[i][j] + (val ? __ldg(&bias[n]) : 0.f);
+    }
+  }
+}
+
+// X[r][k] = sum_n G[r][n] W[n][k]
+__device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ W,
+                        float* __restrict__ X, int R, int N, int K) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  for (int n = 0; n < N; n += 4) {
+    float4 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = ty + 16 * i;
+      a[i] = r < R ? *reinterpret_cast<const float4*>(&Gz[r * LDS + n]) : make_float4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = tx + 16 * j;
+      if (k < K) {
+        const float b0 = W[n * LDS + k], b1 = W[(n + 1) * LDS + k];
+        const float b2 = W[(n + 2) * LDS + k], b3 = W[(n + 3) * LDS + k];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          float v = acc[i][j];
+          v = fmaf(a[i].x, b0, v);
+          v = fmaf(a[i].y, b1, v);
+          v = fmaf(a[i].z, b2, v);
+          v = fmaf(a[i].w, b3, v);
+          acc[i][j] = v;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = ty + 16 * i;
+    if (r >= R) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = tx + 16 * j;
+      if (k < K) X[r * LDS + k] = acc[i][j];
+    }
+  }
+}
+
+// dW[n][k] (+)= sum_r G[r][n] H[r][k]; db[n] (+)= sum over value rows of G[r][n].
+__device__ void gemm_dw(const float* __restrict__ Gz, const float* __restrict__ H,
+                        float* __restrict__ dW, float* __restrict__ db, const DevGroup& G,
+                        int R, int N, int K, bool first) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  for (int r = 0; r < R; ++r) {
+    float ga[8], hb[8];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int n = 4 * ty + 64 * h;
+      const float4 g4 = n < N ? *reinterpret_cast<const float4*>(&Gz[r * LDS + n])
+                              : make_float4(0, 0, 0, 0);
+      ga[4 * h + 0] = g4.x; ga[4 * h + 1] = g4.y; ga[4 * h + 2] = g4.z; ga[4 * h + 3] = g4.w;
+      const int k = 4 * tx + 64 * h;
+      const float4 h4 = k < K ? *reinterpret_cast<const float4*>(&H[r * LDS + k])
+                              : make_float4(0, 0, 0, 0);
+      hb[4 * h + 0] = h4.x; hb[4 * h + 1] = h4.y; hb[4 * h + 2] = h4.z; hb[4 * h + 3] = h4.w;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(ga[i], hb[j], acc[i][j]);
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int n = 4 * ty + 64 * (i >> 2) + (i & 3);
+    if (n >= N) continue;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 4 * tx + 64 * h;
+      if (k >= K) continue;
+      float4* dst = reinterpret_cast<float4*>(&dW[(int64_t)n * K + k]);
+      float4 v = make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
+      if (!first) {
+        const float4 o = *dst;
+        v.x += o.x; v.y += o.y; v.z += o.z; v.w += o.w;
+      }
+      *dst = v;
+    }
+  }
+  // bias gradient: one thread per neuron
+  const int T = G.T;
+  for (int n = threadIdx.x; n < N; n += NT) {
+    float s = 0.f;
+    for (int r = 0; r < R; ++r)
+      if (G.st_order[r / T] == 0) s += Gz[r * LDS + n];
+    db[n] = first ? s : db[n] + s;
+  }
+}
+
+// In place: Z (pre-activations of every stream) -> H (tanh jet). Streams of a site are processed
+// from the highest order down so that lower-order Z values are still intact when read.
+__device__ void jet_forward(float* __restrict__ buf, const DevGroup& G, int N) {
+  const int T = G.T;
+  for (int e = threadIdx.x; e < T * N; e += NT) {
+    const int p = e / N, n = e - p * N;
+    for (int q = 0; q < G.n_sites; ++q) {
+      const int ns = G.site_nstreams[q];
+      const int base = G.site_streams[q][0];
+      float* zb = &buf[(base * T + p) * LDS + n];
+      const float t = tanhf(*zb);
+      if (ns > 1) {
+        const float s1 = 1.f - t * t, s2 = -2.f * t * s1, s3 = s1 * (6.f * t * t - 2.f);
+        for (int m = ns - 1; m >= 1; --m) {
+          const int s = G.site_streams[q][m];
+          float h = 0.f;
+          for (int u = 0; u < G.st_nrule[s]; ++u) {
+            const DevRule& ru = G.rules[s][u];
+            float v = (float)ru.mult * sig_k(ru.k, t, s1, s2, s3, 0.f);
+            for (int i = 0; i < ru.k; ++i) v *= buf[(ru.sub[i] * T + p) * LDS + n];
+            h += v;
+          }
+          buf[(s * T + p) * LDS + n] = h;
+        }
+      }
+      *zb = t;
+    }
+  }
+}
+
+// In place: gbuf holds dL/dH of every stream, zbuf the pre-activations; gbuf becomes dL/dZ.
+// Streams of a site are processed from the value stream up (see DevPull).
+__device__ void jet_backward(const float* __restrict__ zbuf, float* __restrict__ gbuf,
+                             const DevGroup& G, int N) {
+  const int T = G.T;
+  for (int e = threadIdx.x; e < T * N; e += NT) {
+    const int p = e / N, n = e - p * N;
+    for (int q = 0; q < G.n_sites; ++q) {
+      const int ns = G.site_nstreams[q];
+      const int base = G.site_streams[q][0];
+      const float t = tanhf(zbuf[(base * T + p) * LDS + n]);
+      const float s1 = 1.f - t * t;
+      if (ns == 1) {
+        float* g = &gbuf[(base * T + p) * LDS + n];
+        *g = *g * s1;
+        continue;
+      }
+      const float s2 = -2.f * t * s1, s3 = s1 * (6.f * t * t - 2.f);
+      const float s4 = t * s1 * (16.f - 24.f * t * t);
+      for (int m = 0; m < ns; ++m) {
+        const int b = G.site_streams[q][m];
+        float acc = 0.f;
+        const int pf = G.st_pull_first[b];
+        for (int u = 0; u < G.st_npull[b]; ++u) {
+          const DevPull& pl = G.pulls[pf + u];
+          float v = (float)pl.mult * sig_k(pl.kk, t, s1, s2, s3, s4) *
+                    gbuf[(pl.alpha * T + p) * LDS + n];
+          for (int i = 0; i < pl.n_oth; ++i) v *= zbuf[(pl.oth[i] * T + p) * LDS + n];
+          acc += v;
+        }
+        gbuf[(b * T + p) * LDS + n] = acc;
+      }
+    }
+  }
+}
+
+__device__ void load_weights(float* __restrict__ wbuf, const float* __restrict__ W, int N, int K) {
+  const int K4 = K >> 2;
+  for (int e = threadIdx.x; e < N * K4; e += NT) {
+    const int n = e / K4, k = (e - n * K4) * 4;
+    *reinterpret_cast<float4*>(&wbuf[n * LDS + k]) =
+        __ldg(reinterpret_cast<const float4*>(&W[(int64_t)n * K + k]));
+  }
+}
+
+__device__ void copy_rows(float* __restrict__ dst, const float* __restrict__ src, int R, int K) {
+  const int K4 = K >> 2;
+  for (int e = threadIdx.x; e < R * K4; e += NT) {
+    const int r = e / K4, k = (e - r * K4) * 4;
+    *reinterpret_cast<float4*>(&dst[r * LDS + k]) = *reinterpret_cast<const float4*>(&src[r * LDS + k]);
+  }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* bufA = reinterpret_cast<float*>(smem_raw);
+  float* bufB = bufA + RMAX * LDS;
+  float* wbuf = bufB + RMAX * LDS;
+  float* ybuf = wbuf + RMAX * LDS;                  // [RMAX][MAX_OUT]
+  float* gybuf = ybuf + RMAX * MAX_OUT;             // [RMAX][MAX_OUT]
+  float* xsbuf = gybuf + RMAX * MAX_OUT;            // [RMAX][TDG_MAX_DIN]
+  DevGroup* Gs = reinterpret_cast<DevGroup*>(xsbuf + RMAX * TDG_MAX_DIN);
+  double* slot_acc = reinterpret_cast<double*>(
+      (reinterpret_cast<uintptr_t>(Gs + 1) + 15) & ~uintptr_t(15));
+  double* wred = slot_acc + MAX_SLOTS;             // [NT/32][MAX_OUT]
+
+  const int tid = threadIdx.x;
+  const int cta = blockIdx.x;
+  const int L = A.n_layers;
+  const int d_in = A.width[0], d_out = A.width[L];
+  for (int s = tid; s < A.n_slots; s += NT) slot_acc[s] = 0.0;
+  int cur_group = -1;
+  float* scr = A.scratch + (int64_t)cta * (L - 1) * RMAX * LDS;
+
+  for (int ti = A.cta_tile_begin[cta]; ti < A.cta_tile_begin[cta + 1]; ++ti) {
+    const DevTile tile = A.tiles[ti];
+    __syncthreads();
+    if (tile.group != cur_group) {
+      const int4* src = reinterpret_cast<const int4*>(&A.groups[tile.group]);
+      int4* dst = reinterpret_cast<int4*>(Gs);
+      for (int e = tid; e < (int)(sizeof(DevGroup) / 16); e += NT) dst[e] = src[e];
+      cur_group = tile.group;
+      __syncthreads();
+    }
+    const DevGroup& G = *Gs;
+    const int T = G.T, S = G.S, R = T * S;
+    const int nvalid = tile.nvalid, row0 = tile.row0;
+    const float* prm = A.params + (int64_t)G.problem * A.n_params;
+
+    // ---- coordinates of every row (site point + FP32 offset), zero for padding points
+    for (int e = tid; e < R * d_in; e += NT) {
+      const int r = e / d_in, a = e - r * d_in;
+      const int s = r / T, p = r - s * T;
+      const int q = G.st_site[s];
+      float x = 0.f;
+      if (p < nvalid) x = A.arrays[G.site_points[q]][(int64_t)(row0 + p) * d_in + a] + G.site_off[q][a];
+      xsbuf[r * TDG_MAX_DIN + a] = x;
+    }
+    __syncthreads();
+
+    // ---- input layer: value streams W x + b; first-order streams W[:, axis]; higher orders 0
+    {
+      const int N = A.width[1];
+      const float* W0 = prm + A.w_off[0];
+      const float* b0 = prm + A.b_off[0];
+      for (int e = tid; e < R * N; e += NT) {
+        const int r = e / N, n = e - r * N;
+        const int s = r / T;
+        const int o = G.st_order[s];
+        float z;
+        if (o == 0) {
+          z = 0.f;
+          for (int a = 0; a < d_in; ++a) z = fmaf(__ldg(&W0[n * d_in + a]), xsbuf[r * TDG_MAX_DIN + a], z);
+          z += __ldg(&b0[n]);
+        } else if (o == 1) {
+          z = __ldg(&W0[n * d_in + G.st_axis[s]]);
+        } else {
+          z = 0.f;
+        }
+        bufA[r * LDS + n] = z;
+      }
+    }
+    __syncthreads();
+    if (A.do_grad) copy_rows(scr, bufA, R, A.width[1]);
+    jet_forward(bufA, G, A.width[1]);
+    __syncthreads();
+
+    float* hin = bufA;
+    float* hout = bufB;
+    // ---- hidden layers
+    for (int l = 1; l < L - 1; ++l) {
+      const int K = A.width[l], N = A.width[l + 1];
+      load_weights(wbuf, prm + A.w_off[l], N, K);
+      __syncthreads();
+      gemm_fwd(hin, wbuf, hout, prm + A.b_off[l], G, R, N, K);
+      __syncthreads();
+      if (A.do_grad) copy_rows(scr + (int64_t)l * RMAX * LDS, hout, R, N);
+      jet_forward(hout, G, N);
+      __syncthreads();
+      float* t = hin; hin = hout; hout = t;
+    }
+
+    // ---- output layer
+    {
+      const int K = A.width[L - 1];
+      const float* Wl = prm + A.w_off[L - 1];
+      const float* bl = prm + A.b_off[L - 1];
+      for (int e = tid; e < R * d_out; e += NT) {
+        const int r = e / d_out, o = e - r * d_out;
+        float z = 0.f;
+        const float* h = &hin[r * LDS];
+        const float* w = &Wl[(int64_t)o * K];
+        for (int k = 0; k < K; k += 4) {
+          const float4 hv = *reinterpret_cast<const float4*>(&h[k]);
+          z = fmaf(hv.x, __ldg(&w[k]), z);
+          z = fmaf(hv.y, __ldg(&w[k + 1]), z);
+          z = fmaf(hv.z, __ldg(&w[k + 2]), z);
+          z = fmaf(hv.w, __ldg(&w[k + 3]), z);
+        }
+        if (G.st_order[r / T] == 0) z += __ldg(&bl[o]);
+        ybuf[r * MAX_OUT + o] = z;
+        gybuf[r * MAX_OUT + o] = 0.f;
+      }
+    }
+    __syncthreads();
+
+    // ---- operator program, squared error, loss seeds and program adjoint (one thread per point)
+    const int n_out = G.n_outputs;
+    float err2[MAX_OUT];
+#pragma unroll
+    for (int o = 0; o < MAX_OUT; ++o) err2[o] = 0.f;
+    if (tid < T) {
+      const int p = tid;
+      const bool valid = p < nvalid;
+      float outv[MAX_OUT];
+#pragma unroll
+      for (int o = 0; o < MAX_OUT; ++o) outv[o] = 0.f;
+      for (int t = 0; t < G.n_terms; ++t) {
+        const DevTerm& tm = G.terms[t];
+        const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+        float prod = 1.f;
+        for (int f = 0; f < tm.n_factors; ++f) {
+          const DevFactor& fc = G.factors[tm.factor_first + f];
+          float F = 0.f;
+          for (int u = 0; u < fc.n_parts; ++u) {
+            const DevPart& pt = G.parts[fc.part_first + u];
+            F = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, F);
+          }
+          prod *= pow_f(F, fc.power);
+        }
+        outv[tm.output] += c * prod;
+      }
+      float seed[MAX_OUT];
+#pragma unroll
+      for (int o = 0; o < MAX_OUT; ++o) seed[o] = 0.f;
+      for (int o = 0; o < n_out; ++o) {
+        const float tgt = (G.target_array >= 0 && valid)
+                              ? A.arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
+        const float e = valid ? outv[o] - tgt : 0.f;
+        err2[o] = e * e;
+        seed[o] = e * G.seed_scale[o];   // dL/d(out) = 2 * weight * (out - target)
+        if (A.outputs && G.out_offset >= 0 && valid)
+          A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = outv[o];
+      }
+      if (A.do_grad) {
+        for (int t = 0; t < G.n_terms; ++t) {
+          const DevTerm& tm = G.terms[t];
+          const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+          const float dt = seed[tm.output] * c;
+          if (dt == 0.f) continue;
+          float F[MAX_TERM_FACTORS];
+          for (int f = 0; f < tm.n_factors; ++f) {
+            const DevFactor& fc = G.factors[tm.factor_first + f];
+            float v = 0.f;
+            for (int u = 0; u < fc.n_parts; ++u) {
+              const DevPart& pt = G.parts[fc.part_first + u];
+              v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
+            }
+            F[f] = v;
+          }
+          for (int f = 0; f < tm.n_factors; ++f) {
+            const DevFactor& fc = G.factors[tm.factor_first + f];
+            float d = dt * dpow_f(F[f], fc.power);
+            for (int g = 0; g < tm.n_factors; ++g)
+              if (g != f) d *= pow_f(F[g], G.factors[tm.factor_first + g].power);
+            for (int u = 0; u < fc.n_parts; ++u) {
+              const DevPart& pt = G.parts[fc.part_first + u];
+              gybuf[(pt.stream * T + p) * MAX_OUT + fc.var] += d * pt.weight;
+            }
+          }
+        }
+      }
+    }
+    // deterministic FP64 reduction of squared errors: warp shuffle, then warps in order
+    {
+      const int lane = tid & 31, warp = tid >> 5;
+      for (int o = 0; o < n_out; ++o) {
+        double v = (double)err2[o];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) wred[warp * MAX_OUT + o] = v;
+      }
+      __syncthreads();
+      if (tid < n_out) {
+        double s = 0.0;
+        for (int w = 0; w < NT / 32; ++w) s += wred[w * MAX_OUT + tid];
+        slot_acc[G.slot_first + tid] += s;
+      }
+    }
+    if (!A.do_grad) continue;
+    __syncthreads();
+
+    // ---- backward: gybuf holds dL/dY of every (point, stream) row
+    float* grad = A.partial + (int64_t)tile.seg * A.part_stride;
+    const bool first = tile.first_in_seg != 0;
+    // output layer: dW, db, and dL/dH of the last hidden layer into hout
+    {
+      const int K = A.width[L - 1];
+      const float* Wl = prm + A.w_off[L - 1];
+      float* dW = grad + A.w_off[L - 1];
+      float* db = grad + A.b_off[L - 1];
+      for (int e = tid; e < d_out * K; e += NT) {
+        const int o = e / K, k = e - o * K;
+        float s = 0.f;
+        for (int r = 0; r < R; ++r) s = fmaf(gybuf[r * MAX_OUT + o], hin[r * LDS + k], s);
+        dW[(int64_t)o * K + k] = first ? s : dW[(int64_t)o * K + k] + s;
+      }
+      for (int o = tid; o < d_out; o += NT) {
+        float s = 0.f;
+        for (int r = 0; r < R; ++r)
+          if (G.st_order[r / T] == 0) s += gybuf[r * MAX_OUT + o];
+        db[o] = first ? s : db[o] + s;
+      }
+      for (int e = tid; e < R * K; e += NT) {
+        const int r = e / K, k = e - r * K;
+        float s = 0.f;
+        for (int o = 0; o < d_out; ++o) s = fmaf(gybuf[r * MAX_OUT + o], __ldg(&Wl[(int64_t)o * K + k]), s);
+        hout[r * LDS + k] = s;
+      }
+    }
+    __syncthreads();
+    float* gcur = hout;   // dL/dH_l
+    float* other = hin;
+    for (int l = L - 1; l >= 1; --l) {
+      // layer l: H_l = jet(Z_l), Z_l = Linear_{l-1}(H_{l-1}); width[l] neurons
+      const int N = A.width[l];
+      copy_rows(other, scr + (int64_t)(l - 1) * RMAX * LDS, R, N);
+      __syncthreads();
+      jet_backward(other, gcur, G, N);   // gcur: dL/dZ_l
+      __syncthreads();
+      if (l >= 2) {
+        const int K = A.width[l - 1];
+        copy_rows(other, scr + (int64_t)(l - 2) * RMAX * LDS, R, K);
+        load_weights(wbuf, prm + A.w_off[l - 1], N, K);
+        __syncthreads();
+        jet_forward(other, G, K);          // other: H_{l-1}
+        __syncthreads();
+        gemm_dw(gcur, other, grad + A.w_off[l - 1], grad + A.b_off[l - 1], G, R, N, K, first);
+        __syncthreads();
+        gemm_dx(gcur, wbuf, other, R, N, K);   // other: dL/dH_{l-1}
+        __syncthreads();
+        float* t = gcur; gcur = other; other = t;
+      } else {
+        // input layer gradients
+        float* dW0 = grad + A.w_off[0];
+        float* db0 = grad + A.b_off[0];
+        for (int n = tid; n < N; n += NT) {
+          float sb = 0.f;
+          float sw[TDG_MAX_DIN] = {0.f, 0.f, 0.f, 0.f};
+          for (int r = 0; r < R; ++r) {
+            const int s = r / T;
+            const int o = G.st_order[s];
+            const float g = gcur[r * LDS + n];
+            if (o == 0) {
+              sb += g;
+              for (int a = 0; a < d_in; ++a) sw[a] = fmaf(g, xsbuf[r * TDG_MAX_DIN + a], sw[a]);
+            } else if (o == 1) {
+              const int ax = G.st_axis[s];
+              for (int a = 0; a < d_in; ++a) if (a == ax) sw[a] += g;
+            }
+          }
+          for (int a = 0; a < d_in; ++a)
+            dW0[n * d_in + a] = first ? sw[a] : dW0[n * d_in + a] + sw[a];
+          db0[n] = first ? sb : db0[n] + sb;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int s = tid; s < A.n_slots; s += NT) A.slot_partial[(int64_t)cta * A.n_slots + s] = slot_acc[s];
+}
+
+cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s) {
+  static bool attr_set = false;
+  const size_t smem = fused_smem_bytes();
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(fused_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  fused_fp32_kernel<<<n_ctas, NT, smem, s>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace tdg

@@ -1,0 +1,120 @@
+// Internal tables shared by the host-side plan builder (tdg_plan.cu) and the kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/tdg.h"
+
+namespace tdg {
+
+constexpr int NT = 256;            // threads per CTA of the fused kernel
+constexpr int RMAX = 128;          // (point, stream) rows per tile
+constexpr int LDS = 132;           // row stride (floats) of shared-memory activation tiles
+constexpr int SMAX = TDG_MAX_STREAMS;
+constexpr int MAX_SITES = TDG_MAX_SITES;
+constexpr int MAX_RULES = 6;       // Faa di Bruno terms of one stream (order <= 3 needs 5)
+constexpr int MAX_PULL = 160;      // adjoint contributions of one group
+constexpr int MAX_TERMS = 32;
+constexpr int MAX_FACTORS = 64;
+constexpr int MAX_PARTS = 256;
+constexpr int MAX_TERM_FACTORS = 4;
+constexpr int MAX_OUT = TDG_MAX_DOUT;   // outputs per group row
+constexpr int MAX_SLOTS = 1024;    // loss slots of a plan
+
+// H^alpha = sum_rules mult * tanh^(k)(z_base) * prod_{i<k} Z[sub[i]]
+struct DevRule {
+  int8_t k, mult;
+  int8_t sub[3];
+  int8_t pad[3];
+};
+
+// adjoint: G_Z[beta] += mult * tanh^(kk)(z_base) * prod_{i<n_oth} Z[oth[i]] * G_H[alpha]
+struct DevPull {
+  int8_t alpha, kk, mult, n_oth;
+  int8_t oth[3];
+  int8_t pad;
+};
+
+struct DevTerm {
+  int16_t factor_first, n_factors, output, coeff_array;
+  float coeff;
+};
+
+struct DevFactor {
+  int16_t part_first, n_parts, var, pad;
+  float power;
+};
+
+struct DevPart {
+  int16_t stream, pad;
+  float weight;
+};
+
+// Everything the fused kernel needs about one group, copied to shared memory per tile.
+struct alignas(16) DevGroup {
+  int32_t n_rows, T, S, n_sites;
+  int32_t n_outputs, n_terms, problem, slot_first;
+  int32_t target_array, pad0;
+  int64_t out_offset;
+  float seed_scale[MAX_OUT];              // 2 * loss weight of each output's slot
+  int32_t site_points[MAX_SITES];
+  float site_off[MAX_SITES][TDG_MAX_DIN];
+  int8_t site_nstreams[MAX_SITES];
+  int8_t site_streams[MAX_SITES][SMAX];   // row-stream indices of a site, increasing order; [0] = value
+  int8_t st_site[SMAX], st_order[SMAX], st_axis[SMAX], st_nrule[SMAX];
+  int8_t st_npull[SMAX];
+  int16_t st_pull_first[SMAX];
+  DevRule rules[SMAX][MAX_RULES];
+  DevPull pulls[MAX_PULL];
+  DevTerm terms[MAX_TERMS];
+  DevFactor factors[MAX_FACTORS];
+  DevPart parts[MAX_PARTS];
+};
+
+struct DevTile {
+  int32_t group, row0, nvalid, seg;
+  int32_t first_in_seg, pad[3];
+};
+
+static_assert(sizeof(DevGroup) % 16 == 0, "DevGroup is copied as int4");
+
+struct FusedArgs {
+  const DevGroup* groups;
+  const DevTile* tiles;
+  const int32_t* cta_tile_begin;      // n_ctas + 1
+  const float* const* arrays;         // device table of device pointers
+  const float* params;                // n_problems x n_params
+  int64_t n_params;                   // per problem
+  int64_t part_stride;                // floats per gradient segment (n_params rounded up to 4)
+  float* partial;                     // n_segments x part_stride
+  double* slot_partial;               // n_ctas x n_slots
+  int32_t n_slots;
+  int32_t do_grad;
+  float* outputs;                     // optional
+  float* scratch;                     // n_ctas x (n_layers-1) x RMAX x LDS
+  int32_t n_layers;
+  int32_t width[TDG_MAX_LAYERS + 1];
+  int64_t w_off[TDG_MAX_LAYERS], b_off[TDG_MAX_LAYERS];
+};
+
+// shared-memory bytes of the fused FP32 kernel
+constexpr size_t fused_smem_bytes() {
+  return sizeof(float) * (3 * RMAX * LDS + 2 * RMAX * MAX_OUT + RMAX * TDG_MAX_DIN)
+         + sizeof(DevGroup) + sizeof(double) * (MAX_SLOTS + NT / 32 * MAX_OUT) + 64;
+}
+
+cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s);
+cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
+                               const int32_t* seg_list, int n_problems, int64_t n_params,
+                               float* grad, cudaStream_t s);
+cudaError_t launch_reduce_loss(const double* slot_partial, int n_ctas, int n_slots,
+                               const int32_t* slot_problem, const double* slot_w,
+                               const double* slot_wn, int n_problems, double* loss,
+                               cudaStream_t s);
+cudaError_t launch_adam(float* p, const float* g, float* m, float* v, float* step, int64_t n,
+                        const tdg_adam_desc& hp, cudaStream_t s);
+cudaError_t launch_dot_f64(const float* a, const float* b, int64_t n, double* out,
+                           cudaStream_t s);
+
+void count_launch(int n = 1);
+
+}  // namespace tdg

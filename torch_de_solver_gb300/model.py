@@ -1,0 +1,126 @@
+"""Model: compile() and train() with the reference's signatures (tedeous/model.py:25-195).
+
+compile() builds the grid, evaluates boundary data, lowers the operator and boundary conditions
+(prepare.lower) and creates the device plan behind a Solution. train() keeps the reference's loop:
+an initial evaluate(), then epochs - 1 optimizer steps, callbacks around every epoch
+(tedeous/model.py:154-193). With the fused Adam and no learning-rate scheduler, each step
+(loss + gradient kernel, reductions, Adam update) is captured once in a CUDA graph and replayed.
+"""
+
+import datetime
+import os
+import tempfile
+from typing import List, Union
+
+import torch
+
+from .callbacks import CallbackList
+from .closure import Closure
+from .data import Conditions, Domain, Equation
+from .optimizer import FusedAdam, Optimizer
+from .solution import Solution
+
+
+class Model:
+    def __init__(self, net: torch.nn.Module, domain: Domain, equation: Equation,
+                 conditions: Conditions, batch_size: int = None):
+        self.net = net
+        self.domain = domain
+        self.equation = equation
+        self.conditions = conditions
+        self.batch_size = batch_size
+        self._save_dir = os.path.join(tempfile.gettempdir(), 'tedeous_cache/')
+        self._graph = None
+
+    def compile(self, mode: str, lambda_operator: Union[List[float], float],
+                lambda_bound: Union[List[float], float], normalized_loss_stop: bool = False,
+                h: float = 0.001, inner_order: str = '1', boundary_order: str = '2',
+                derivative_points: int = 2, weak_form: List[callable] = None, tol: float = 0,
+                removed_domains: list = None, precision: str = 'fp32', form: str = 'fused'):
+        """Arguments as in tedeous/model.py:56-113, plus precision ('fp32') and form ('fused')."""
+        if weak_form:
+            raise NotImplementedError('weak-form losses are not implemented on the device path')
+        if tol:
+            raise NotImplementedError('the causal loss (tol > 0) is not implemented on the '
+                                      'device path')
+        if self.batch_size is not None:
+            raise NotImplementedError('mini-batch training is not implemented on the device path')
+        self.mode = mode
+        self.lambda_bound = lambda_bound
+        self.lambda_operator = lambda_operator
+        self.normalized_loss_stop = normalized_loss_stop
+        self.weak_form = weak_form
+        grid = self.domain.build(mode=mode, removed_domains=removed_domains)
+        bconds = self.conditions.build(self.domain.variable_dict)
+        self.solution_cls = Solution(grid, self.equation.equation_lst, bconds, self.net, mode,
+                                     lambda_operator, lambda_bound, h=h, inner_order=inner_order,
+                                     boundary_order=boundary_order, precision=precision, form=form)
+        self.net = self.solution_cls.model
+        self._graph = None
+
+    def _model_save(self, save_model: bool, model_name: str):
+        if save_model:
+            os.makedirs(self._save_dir, exist_ok=True)
+            name = model_name or str(datetime.datetime.now().timestamp())
+            torch.save({'model': self.net, 'model_state_dict': self.net.state_dict()},
+                       os.path.join(self._save_dir, name + '.tar'))
+
+    def _fused_step(self, capture: bool):
+        """loss+gradient, Adam; returns the (1,) loss seen before the update."""
+        sol, opt = self.solution_cls, self.optimizer
+        if self._graph is not None:
+            self._graph.replay()
+            return self._loss32[0:1]
+        sol._sync_params()
+        sol.plan.loss_grad(sol.flat, sol._grad, sol._loss_buf, sol._outputs)
+        opt.apply(sol._grad)
+        if capture:
+            self._loss32 = torch.empty(2, device=sol.device)
+            stream = torch.cuda.Stream(sol.device)
+            stream.wait_stream(torch.cuda.current_stream(sol.device))
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                sol.plan.loss_grad(sol.flat, sol._grad, sol._loss_buf, sol._outputs)
+                self._loss32.copy_(sol._loss_buf)
+                opt.apply(sol._grad)
+            self._graph = g
+            # the captured work did not run: the eager step above already advanced one step
+        return sol._loss_buf[0:1].to(torch.float32)
+
+    def train(self, optimizer: Optimizer, epochs: int, info_string_every: Union[int, None] = None,
+              mixed_precision: bool = False, save_model: bool = False,
+              model_name: Union[str, None] = None, callbacks: Union[List, None] = None):
+        if mixed_precision:
+            raise NotImplementedError('mixed_precision: choose compile(precision=...) instead')
+        self.t = 1
+        self.stop_training = False
+        cbs = CallbackList(callbacks=callbacks, model=self)
+        cbs.on_train_begin()
+        self.net = self.solution_cls.model
+        self.optimizer = optimizer.optimizer_choice(self.mode, self.net)
+        closure = Closure(mixed_precision, self).get_closure(optimizer.optimizer)
+        self.min_loss, _ = self.solution_cls.evaluate()
+        self.cur_loss = self.min_loss
+        print('[{}] initial (min) loss is {}'.format(datetime.datetime.now(), self.min_loss.item()))
+        fused = (isinstance(self.optimizer, FusedAdam) and optimizer.gamma is None
+                 and optimizer.cosine_scheduler_patience is None and not self.normalized_loss_stop)
+        self._graph = None
+        n_eager = 0
+        while self.t < epochs and self.stop_training is False:
+            cbs.on_epoch_begin()
+            self.optimizer.zero_grad()
+            if fused:
+                loss = self._fused_step(capture=(n_eager == 2))
+                n_eager += 1
+                self.cur_loss = loss.clone() if cbs.callbacks else loss
+            else:
+                self.optimizer.step(closure)
+                if optimizer.gamma is not None and self.t % optimizer.decay_every == 0:
+                    optimizer.scheduler.step()
+            cbs.on_epoch_end()
+            self.t += 1
+            if info_string_every is not None and self.t % info_string_every == 0:
+                print('This parameter info_string_every in train is obstolete, please use callbacks')
+        self._graph = None
+        cbs.on_train_end()
+        self._model_save(save_model, model_name)

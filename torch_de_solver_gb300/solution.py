@@ -1,0 +1,295 @@
+"""Solution: the per-step loss evaluation, backed by libtdg.so.
+
+Drop-in for the reference's Solution (tedeous/solution.py:19-168): evaluate() returns
+(loss, loss_normalized) as shape-(1,) tensors, and loss.backward() fills .grad of every MLP
+parameter, so the reference's closure (tedeous/optimizers/closure.py:49-64) and torch optimizers
+work unchanged. The attributes op, bval, true_bval, bval_keys and bval_length that callbacks read
+are rebuilt on access from the per-row outputs the kernel writes.
+
+The MLP parameters are re-seated as views into one flat FP32 device buffer, which the kernel
+reads directly; the gradient comes back as one flat buffer and is handed to autograd as
+per-parameter views.
+"""
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .prepare import lower
+
+
+def mlp_widths(net):
+    """Widths of a torch.nn.Sequential of Linear layers separated by Tanh."""
+    mods = list(net.children()) if isinstance(net, torch.nn.Sequential) else None
+    if not mods:
+        raise NotImplementedError('the device path needs a torch.nn.Sequential of Linear/Tanh')
+    widths = []
+    for i, m in enumerate(mods):
+        if i % 2 == 0:
+            if not isinstance(m, torch.nn.Linear) or m.bias is None:
+                raise NotImplementedError(f'layer {i}: expected Linear with bias, got {m}')
+            if not widths:
+                widths.append(m.in_features)
+            elif m.in_features != widths[-1]:
+                raise ValueError('inconsistent Linear widths')
+            widths.append(m.out_features)
+        elif not isinstance(m, torch.nn.Tanh):
+            raise NotImplementedError(f'layer {i}: only Tanh activations are implemented, got {m}')
+    if len(mods) % 2 == 0:
+        raise NotImplementedError('the network must end with a Linear layer')
+    return widths
+
+
+def flatten_parameters(net, device):
+    """Move `net` to `device` and make its parameters views of one flat float32 buffer
+    (torch.nn.Module.parameters() order: W0, b0, W1, b1, ...)."""
+    params = list(net.parameters())
+    flat = torch.cat([p.detach().reshape(-1).to(device=device, dtype=torch.float32)
+                      for p in params])
+    off = 0
+    with torch.no_grad():
+        for p in params:
+            n = p.numel()
+            p.data = flat[off:off + n].view(p.shape)
+            off += n
+    return flat
+
+
+def params_are_views(net, flat):
+    off = 0
+    for p in net.parameters():
+        if p.data.data_ptr() != flat.data_ptr() + 4 * off or p.dtype != torch.float32:
+            return False
+        off += p.numel()
+    return off == flat.numel()
+
+
+class DevicePlan:
+    """A tdg_plan for one or more lowered problems (ProblemIR) sharing one MLP shape."""
+
+    def __init__(self, irs, widths, device, precision='fp32', form='fused'):
+        if precision not in _lib.PREC:
+            raise ValueError(f'precision {precision!r}')
+        if form not in _lib.FORM:
+            raise ValueError(f'form {form!r}')
+        lib = _lib.load()
+        self.device = device
+        self.widths = list(widths)
+        streams, sites, parts, factors, terms, groups, slots = [], [], [], [], [], [], []
+        self.arrays = []
+        self.group_out = []          # per problem: list of (group, output offset) in IR order
+        out_off = 0
+        for prob, ir in enumerate(irs):
+            base = len(self.arrays)
+            self.arrays += [a.to(device).reshape(-1).contiguous() for a in ir.arrays]
+            slot_base = len(slots)
+            slots += [(prob, w, wn) for (_, w, wn) in ir.slots]
+            offs = []
+            for g in ir.groups:
+                site_first = len(sites)
+                for s in g.sites:
+                    st_first = len(streams)
+                    for axes in s.streams:
+                        ax = list(axes) + [0] * (_lib.MAX_ORDER - len(axes))
+                        streams.append(_lib.StreamDesc(len(axes), (ctypes.c_int32 * 3)(*ax)))
+                    off = list(s.offset) + [0.0] * (_lib.MAX_DIN - len(s.offset))
+                    sites.append(_lib.SiteDesc(base + s.points, st_first, len(s.streams),
+                                               (ctypes.c_float * _lib.MAX_DIN)(*off)))
+                term_first = len(terms)
+                for coeff, output, fl in g.terms:
+                    f_first = len(factors)
+                    for var, pw, pl in fl:
+                        p_first = len(parts)
+                        for site, stream, w in pl:
+                            parts.append(_lib.PartDesc(site, stream, w))
+                        factors.append(_lib.FactorDesc(p_first, len(pl), var, pw))
+                    if isinstance(coeff, float):
+                        terms.append(_lib.TermDesc(f_first, len(fl), output, -1, coeff))
+                    else:
+                        terms.append(_lib.TermDesc(f_first, len(fl), output, base + coeff, 0.0))
+                tgt = -1 if g.target is None else base + g.target
+                groups.append(_lib.GroupDesc(prob, g.n_rows, site_first, len(g.sites), term_first,
+                                             len(g.terms), g.n_outputs, slot_base + g.slot_first,
+                                             tgt, out_off))
+                offs.append(out_off)
+                out_off += g.n_rows * g.n_outputs
+            self.group_out.append(offs)
+        self.n_outputs_total = out_off
+        self.n_problems = len(irs)
+
+        def arr(ctype, items):
+            a = (ctype * max(1, len(items)))()
+            for i, x in enumerate(items):
+                a[i] = x
+            return a
+        self._keep = dict(
+            streams=arr(_lib.StreamDesc, streams), sites=arr(_lib.SiteDesc, sites),
+            parts=arr(_lib.PartDesc, parts), factors=arr(_lib.FactorDesc, factors),
+            terms=arr(_lib.TermDesc, terms), groups=arr(_lib.GroupDesc, groups),
+            slots=arr(_lib.SlotDesc, [_lib.SlotDesc(p, w, wn) for p, w, wn in slots]),
+            ptrs=arr(ctypes.c_void_p, [t.data_ptr() for t in self.arrays]),
+            lens=arr(ctypes.c_int64, [t.numel() for t in self.arrays]))
+        k = self._keep
+        mlp = _lib.MlpDesc()
+        mlp.n_layers = len(widths) - 1
+        for i, w in enumerate(widths):
+            mlp.width[i] = w
+        desc = _lib.ProblemDesc(
+            mlp, len(irs), len(groups), k['groups'], len(sites), k['sites'], len(streams),
+            k['streams'], len(terms), k['terms'], len(factors), k['factors'], len(parts),
+            k['parts'], len(slots), k['slots'], len(self.arrays), k['ptrs'], k['lens'],
+            _lib.PREC[precision], _lib.FORM[form])
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(device):
+            _lib.check(lib.tdg_plan_create(ctypes.byref(desc), ctypes.byref(handle)),
+                       'tdg_plan_create')
+        self.handle = handle
+        info = _lib.PlanInfo()
+        _lib.check(lib.tdg_plan_get_info(handle, ctypes.byref(info)), 'tdg_plan_get_info')
+        self.info = info
+        self.n_params = int(info.n_params)
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h is not None and h.value:
+            try:
+                _lib.load().tdg_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def set_array(self, index, tensor):
+        _lib.check(_lib.load().tdg_plan_set_array(self.handle, index, tensor.data_ptr(),
+                                                  tensor.numel()), 'tdg_plan_set_array')
+
+    def loss_grad(self, params, grad, loss, outputs=None, stream=None):
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        _lib.check(_lib.load().tdg_loss_grad(
+            self.handle, params.data_ptr(), grad.data_ptr(), loss.data_ptr(),
+            None if outputs is None else outputs.data_ptr(), s.cuda_stream), 'tdg_loss_grad')
+
+    def loss(self, params, loss, outputs=None, stream=None):
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        _lib.check(_lib.load().tdg_loss(
+            self.handle, params.data_ptr(), loss.data_ptr(),
+            None if outputs is None else outputs.data_ptr(), s.cuda_stream), 'tdg_loss')
+
+
+class _FusedLoss(torch.autograd.Function):
+    """(loss, loss_normalized) of the current parameters; the gradient is computed in the same
+    fused launch and returned, scaled by the incoming gradient, in backward()."""
+
+    @staticmethod
+    def forward(ctx, sol, *params):
+        sol._launch(with_grad=True)
+        ctx.sol = sol
+        grad = sol._grad.clone() if sol._clone_grad else sol._grad
+        ctx.save_for_backward(grad)
+        loss = sol._loss_buf[0:1].to(torch.float32)
+        lossn = sol._loss_buf[1:2].to(torch.float32)
+        ctx.mark_non_differentiable(lossn)
+        return loss, lossn
+
+    @staticmethod
+    def backward(ctx, g_loss, g_lossn):
+        grad, = ctx.saved_tensors
+        g = grad * g_loss.reshape(()).to(grad.dtype)
+        out = []
+        off = 0
+        for shape, n in ctx.sol._shapes:
+            out.append(g[off:off + n].view(shape))
+            off += n
+        return (None, *out)
+
+
+class Solution:
+    """Loss evaluation of one compiled problem (tedeous/solution.py:19-168)."""
+
+    def __init__(self, grid, operator, bconds, model, mode, lambda_operator, lambda_bound,
+                 h=0.001, inner_order='1', boundary_order='2', precision='fp32', form='fused',
+                 device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
+        self.device = torch.device('cuda', torch.cuda.current_device()) if device is None \
+            else torch.device(device)
+        self.mode = mode
+        self.grid = grid
+        self.lambda_operator, self.lambda_bound = lambda_operator, lambda_bound
+        widths = mlp_widths(model)
+        self.ir = lower(grid, operator, bconds, mode, lambda_operator, lambda_bound, h,
+                        inner_order, boundary_order, d_out=widths[-1])
+        self.model = model.to(self.device)
+        self.flat = flatten_parameters(self.model, self.device)
+        self._shapes = [(p.shape, p.numel()) for p in self.model.parameters()]
+        self.plan = DevicePlan([self.ir], widths, self.device, precision, form)
+        self._grad = torch.zeros(self.plan.n_params, device=self.device, dtype=torch.float32)
+        self._loss_buf = torch.zeros(2, device=self.device, dtype=torch.float64)
+        self._outputs = torch.zeros(max(1, self.plan.n_outputs_total), device=self.device)
+        self._clone_grad = True
+        self.bval_keys = list(self.ir.bc_types)
+        self.bval_length = [sum(r for _, r in self.ir.bc_parts[t]) for t in self.ir.bc_types]
+        self._true_bval = None
+
+    # -- parameters --------------------------------------------------------------------------
+    def _model_change(self, new_model):
+        """Swap in another network of the same shape (tedeous/solution.py:109-127)."""
+        if mlp_widths(new_model) != self.plan.widths:
+            raise ValueError('new model has a different shape')
+        self.model = new_model.to(self.device)
+        self.flat = flatten_parameters(self.model, self.device)
+
+    def _sync_params(self):
+        if not params_are_views(self.model, self.flat):
+            self.flat = flatten_parameters(self.model, self.device)
+
+    # -- evaluation --------------------------------------------------------------------------
+    def _launch(self, with_grad):
+        if with_grad:
+            self.plan.loss_grad(self.flat, self._grad, self._loss_buf, self._outputs)
+        else:
+            self.plan.loss(self.flat, self._loss_buf, self._outputs)
+
+    def evaluate(self, save_graph: bool = True):
+        """(loss, loss_normalized), each of shape (1,) like the reference's."""
+        self._sync_params()
+        params = list(self.model.parameters())
+        if save_graph and torch.is_grad_enabled() and any(p.requires_grad for p in params):
+            self.loss, self.loss_normalized = _FusedLoss.apply(self, *params)
+        else:
+            self._launch(with_grad=False)
+            self.loss = self._loss_buf[0:1].to(torch.float32)
+            self.loss_normalized = self._loss_buf[1:2].to(torch.float32)
+        return self.loss, self.loss_normalized
+
+    # -- fields read by callbacks ------------------------------------------------------------
+    @property
+    def op(self):
+        ir = self.ir
+        off = self.plan.group_out[0][ir.residual_group]
+        return self._outputs[off:off + ir.n_residual_rows * ir.n_eq].view(-1, ir.n_eq).clone()
+
+    def _bc_columns(self, true):
+        ir = self.ir
+        cols = []
+        for t in ir.bc_types:
+            if true:
+                v = torch.cat([x.reshape(-1) for x in ir.bc_true[t]]).to(self.device)
+            else:
+                pieces = []
+                for gi, n in ir.bc_parts[t]:
+                    off = self.plan.group_out[0][gi]
+                    pieces.append(self._outputs[off:off + n])
+                v = torch.cat(pieces)
+            cols.append(torch.nn.functional.pad(v, (0, ir.max_len - v.numel())))
+        return torch.stack(cols, 1)
+
+    @property
+    def bval(self):
+        return self._bc_columns(False)
+
+    @property
+    def true_bval(self):
+        if self._true_bval is None:
+            self._true_bval = self._bc_columns(True)
+        return self._true_bval
