@@ -207,6 +207,21 @@ tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float
 tdg_status tdg_dot_f64(const float* a, const float* b, int64_t n, double* out,
                        tdg_stream_t stream);
 
+/* Allocation-free variant of tdg_dot_f64. No counterpart in the reference: it serves callers that
+ * own all device memory themselves (a framework allocator that has reserved the GPU, or a
+ * foreign-language host binding this ABI under a fixed device-memory budget) and so cannot let
+ * the library call cudaMalloc, which tdg_dot_f64 does on its first call on each device.
+ * Partial sums live in a static device array of TDG_DOT_NOALLOC_MAX_BLOCKS doubles (32 KiB,
+ * held by every GPU that loads the library until exit); n above TDG_DOT_NOALLOC_MAX_N is
+ * rejected with TDG_ERR_SHAPE. The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture. All calls share the array, so calls that overlap on the GPU race on it. */
+#define TDG_DOT_NOALLOC_MAX_BLOCKS 4096
+#define TDG_DOT_NOALLOC_CHUNK 16384LL
+#define TDG_DOT_NOALLOC_MAX_N (TDG_DOT_NOALLOC_MAX_BLOCKS * TDG_DOT_NOALLOC_CHUNK)
+tdg_status tdg_dot_f64_noalloc(const float* a, const float* b, int64_t n, double* out,
+                               tdg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,7 +99,9 @@ SIGNATURES = {
     'tdg_loss_grad': (i32, [vp, vp, vp, vp, vp, vp]),
     'tdg_adam_step': (i32, [vp, vp, vp, vp, vp, i64, ctypes.POINTER(AdamDesc), vp]),
     'tdg_dot_f64': (i32, [vp, vp, i64, vp, vp]),
+    'tdg_dot_f64_noalloc': (i32, [vp, vp, i64, vp, vp]),
 }
+DOT_NOALLOC_MAX_N = 4096 * 16384
 
 _lib = None
 

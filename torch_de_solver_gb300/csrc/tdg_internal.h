@@ -116,5 +116,7 @@ cudaError_t launch_dot_f64(const float* a, const float* b, int64_t n, double* ou
                            cudaStream_t s);
 
 void count_launch(int n = 1);
+// record the message of a failure for tdg_last_error() and return its status
+tdg_status record_error(tdg_status st, const char* fmt, ...);
 
 }  // namespace tdg

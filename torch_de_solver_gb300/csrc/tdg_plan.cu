@@ -29,6 +29,16 @@ static tdg_status fail(tdg_status st, const char* fmt, ...) {
   return st;
 }
 
+tdg_status record_error(tdg_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return st;
+}
+
 static tdg_status cuda_fail(cudaError_t e, const char* what) {
   return fail(TDG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
