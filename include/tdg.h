@@ -198,6 +198,10 @@ tdg_status tdg_loss(tdg_plan* plan, const float* params, double* loss, float* ou
 tdg_status tdg_loss_grad(tdg_plan* plan, const float* params, float* grad, double* loss,
                          float* outputs, tdg_stream_t stream);
 
+/* Synchronise the device and report TDG_ERR_TIMEOUT if a kernel of this plan gave up a bounded
+ * wait on an mbarrier (the tensor-core path never spins without a limit). */
+tdg_status tdg_plan_sync_status(tdg_plan* plan);
+
 /* In-place Adam (torch.optim.Adam semantics, L2 weight_decay) on n floats; step is a device
  * float counter incremented by the call, so the call can be replayed from a CUDA graph. */
 tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float* exp_avg_sq,

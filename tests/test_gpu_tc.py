@@ -1,0 +1,44 @@
+"""Tensor-core (tcgen05) precisions: TF32 and BF16 hidden GEMMs with FP32 accumulation.
+
+Each variant's loss and gradient are compared with the reference's FP64 fixtures; the measured
+relative errors are printed. Bounds: TF32 1e-2 (10-bit mantissa operands), BF16 1e-1 (7-bit), the
+stated limits these precisions are measured against."""
+import numpy as np
+import pytest
+import torch
+
+import cases
+from helpers import build_model, golden, rel
+
+BOUND = {'tf32': 1e-2, 'bf16': 1e-1}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', ['tf32', 'bf16'])
+@pytest.mark.parametrize('name', list(cases.GOLDEN_CASES))
+def test_tensor_core_precision_against_reference(name, precision):
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300 import _lib
+    g = golden(name)
+    model = build_model(T, name, weights=g['weights'], precision=precision)
+    sol = model.solution_cls
+    loss, lossn = sol.evaluate()
+    loss.backward()
+    _lib.check(_lib.load().tdg_plan_sync_status(sol.plan.handle), 'tdg_plan_sync_status')
+    grad = torch.cat([p.grad.reshape(-1) for p in model.net.parameters()]).cpu().numpy()
+    rl, rg = rel(loss.item(), g['loss64']), rel(grad, g['grad64'])
+    print(f'{name} {precision}: loss rel {rl:.3e} grad rel {rg:.3e}')
+    assert np.isfinite(grad).all()
+    assert rl < BOUND[precision] and rg < BOUND[precision], (rl, rg)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', ['tf32', 'bf16'])
+def test_tensor_core_forward_only_equals_fused(precision):
+    import torch_de_solver_gb300 as T
+    g = golden('kovasznay_ag')
+    model = build_model(T, 'kovasznay_ag', weights=g['weights'], precision=precision)
+    with torch.no_grad():
+        l0, _ = model.solution_cls.evaluate()
+    l1, _ = model.solution_cls.evaluate()
+    assert abs(l0.item() - l1.item()) <= 1e-6 * abs(l1.item())

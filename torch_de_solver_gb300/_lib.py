@@ -97,6 +97,7 @@ SIGNATURES = {
     'tdg_plan_set_array': (i32, [vp, i32, vp, i64]),
     'tdg_loss': (i32, [vp, vp, vp, vp, vp]),
     'tdg_loss_grad': (i32, [vp, vp, vp, vp, vp, vp]),
+    'tdg_plan_sync_status': (i32, [vp]),
     'tdg_adam_step': (i32, [vp, vp, vp, vp, vp, i64, ctypes.POINTER(AdamDesc), vp]),
     'tdg_dot_f64': (i32, [vp, vp, i64, vp, vp]),
     'tdg_dot_f64_noalloc': (i32, [vp, vp, i64, vp, vp]),

@@ -103,6 +103,19 @@ constexpr size_t fused_smem_bytes() {
 }
 
 cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s);
+
+// tensor-core path: packed hidden weights (per hidden Linear j: W_j as an np x kp K-major operand
+// at fwd_off[j] and W_j^T as kp x np at bwd_off[j], widths padded to 16) and a timeout flag
+struct TcLaunch {
+  bool bf16;
+  unsigned char* wpack;
+  int64_t fwd_off[TDG_MAX_LAYERS], bwd_off[TDG_MAX_LAYERS];
+  int64_t w_off[TDG_MAX_LAYERS];
+  int32_t width[TDG_MAX_LAYERS + 1];
+  int* err;
+};
+size_t fused_tc_smem_bytes();
+cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
 cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
                                const int32_t* seg_list, int n_problems, int64_t n_params,
                                float* grad, cudaStream_t s);

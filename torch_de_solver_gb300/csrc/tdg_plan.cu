@@ -71,6 +71,9 @@ struct tdg_plan {
   double* d_slot_w = nullptr;
   double* d_slot_wn = nullptr;
   float* d_scratch = nullptr;
+  unsigned char* d_wpack = nullptr;
+  int* d_err = nullptr;
+  int64_t wpack_fwd[TDG_MAX_LAYERS] = {0}, wpack_bwd[TDG_MAX_LAYERS] = {0};
   int64_t workspace_bytes = 0;
   bool arrays_dirty = false;
 };
@@ -124,7 +127,7 @@ tdg_status dev_alloc(tdg_plan* p, void** dst, size_t bytes) {
 void free_plan(tdg_plan* p) {
   void* ptrs[] = {p->d_groups, p->d_tiles, p->d_cta_begin, (void*)p->d_arrays, p->d_seg_begin,
                   p->d_seg_list, p->d_partial, p->d_slot_partial, p->d_slot_problem,
-                  p->d_slot_w, p->d_slot_wn, p->d_scratch};
+                  p->d_slot_w, p->d_slot_wn, p->d_scratch, p->d_wpack, p->d_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -324,7 +327,8 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     const int w = d.mlp.width[l];
     if (w < 4 || w > TDG_MAX_WIDTH || w % 4) return fail(TDG_ERR_UNSUPPORTED, "hidden width %d (multiple of 4, <= %d)", w, TDG_MAX_WIDTH);
   }
-  if (d.precision != TDG_PREC_FP32) return fail(TDG_ERR_UNSUPPORTED, "precision %d not built", d.precision);
+  if (d.precision != TDG_PREC_FP32 && d.precision != TDG_PREC_TF32 && d.precision != TDG_PREC_BF16)
+    return fail(TDG_ERR_UNSUPPORTED, "precision %d not built", d.precision);
   if (d.form != TDG_FORM_FUSED) return fail(TDG_ERR_UNSUPPORTED, "form %d not built", d.form);
   if (d.n_problems < 1) return fail(TDG_ERR_INVALID, "n_problems < 1");
   if (d.n_groups < 1) return fail(TDG_ERR_INVALID, "no groups");
@@ -428,9 +432,24 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
       (st = dev_upload(p, &p->d_slot_wn, slot_wn.data(), slot_wn.size())) ||
       (st = dev_alloc(p, (void**)&p->d_partial, sizeof(float) * p->part_stride * n_seg)) ||
       (st = dev_alloc(p, (void**)&p->d_slot_partial, sizeof(double) * (size_t)n_ctas * d.n_slots)) ||
-      (st = dev_alloc(p, (void**)&p->d_scratch, sizeof(float) * (size_t)n_ctas * (L - 1) * RMAX * LDS))) {
+      (st = dev_alloc(p, (void**)&p->d_scratch, sizeof(float) * (size_t)n_ctas * (L - 1) * RMAX * LDS)) ||
+      (st = dev_alloc(p, (void**)&p->d_err, sizeof(int)))) {
     free_plan(p);
     return st;
+  }
+  if (cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) { free_plan(p); return fail(TDG_ERR_CUDA, "cudaMemset"); }
+  if (d.precision != TDG_PREC_FP32) {
+    // packed hidden weights for the tensor-core kernel: forward and transposed operand per layer
+    const int es = d.precision == TDG_PREC_BF16 ? 2 : 4;
+    int64_t off = 0;
+    for (int j = 1; j < L - 1; ++j) {
+      const int64_t kp = (d.mlp.width[j] + 15) / 16 * 16, np = (d.mlp.width[j + 1] + 15) / 16 * 16;
+      p->wpack_fwd[j] = off;
+      off += np * kp * es;
+      p->wpack_bwd[j] = off;
+      off += np * kp * es;
+    }
+    if ((st = dev_alloc(p, (void**)&p->d_wpack, (size_t)std::max<int64_t>(off, 16)))) { free_plan(p); return st; }
   }
   *out = p;
   return TDG_OK;
@@ -488,7 +507,26 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
   a.n_layers = p->n_layers;
   for (int l = 0; l <= p->n_layers; ++l) a.width[l] = p->width[l];
   for (int l = 0; l < p->n_layers; ++l) { a.w_off[l] = p->w_off[l]; a.b_off[l] = p->b_off[l]; }
-  cudaError_t e = launch_fused_fp32(a, p->n_ctas, s);
+  cudaError_t e;
+  if (p->precision == TDG_PREC_FP32) {
+    e = launch_fused_fp32(a, p->n_ctas, s);
+  } else {
+    TcLaunch t{};
+    t.bf16 = p->precision == TDG_PREC_BF16;
+    t.wpack = p->d_wpack;
+    for (int l = 0; l < TDG_MAX_LAYERS; ++l) {
+      t.fwd_off[l] = p->wpack_fwd[l];
+      t.bwd_off[l] = p->wpack_bwd[l];
+      t.w_off[l] = p->w_off[l];
+    }
+    for (int l = 0; l <= p->n_layers; ++l) t.width[l] = p->width[l];
+    t.err = p->d_err;
+    if (do_grad) {   // the tensor-core kernel accumulates hidden dW with atomic adds
+      e = cudaMemsetAsync(p->d_partial, 0, sizeof(float) * p->part_stride * p->n_segments, s);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+    e = launch_fused_tc(a, t, p->n_ctas, s);
+  }
   if (e != cudaSuccess) return cuda_fail(e, "fused kernel launch");
   if (do_grad) {
     e = launch_reduce_grad(p->d_partial, p->part_stride, p->d_seg_begin, p->d_seg_list,
@@ -509,6 +547,17 @@ tdg_status tdg_loss(tdg_plan* p, const float* params, double* loss, float* outpu
 tdg_status tdg_loss_grad(tdg_plan* p, const float* params, float* grad, double* loss,
                          float* outputs, tdg_stream_t stream) {
   return run(p, params, grad, loss, outputs, stream, true);
+}
+
+tdg_status tdg_plan_sync_status(tdg_plan* p) {
+  if (!p) return fail(TDG_ERR_INVALID, "null plan");
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize");
+  int flag = 0;
+  e = cudaMemcpy(&flag, p->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy");
+  if (flag) return fail(TDG_ERR_TIMEOUT, "a bounded device wait gave up (code %d)", flag);
+  return TDG_OK;
 }
 
 tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float* exp_avg_sq,
