@@ -40,6 +40,8 @@ WORKLOADS = {
     'burgers': ('burgers_ag', dict(n=100), dict(n=100), 'burgers_autograd_2-32x4-1_101x101'),
     'kdv': ('kdv_ag', dict(nx=255, nt=127), dict(nx=63, nt=31), 'kdv_autograd_2-64x4-1_256x128'),
     'heat': ('heat_nn', dict(n=20), dict(n=20), 'heat_nn_2-100x3-1_21x21'),
+    'sweep': ('sweep_ag', dict(n_solves=256), dict(n_solves=2),
+              'sweep_256_solves_autograd_2-64x3-1_Nx,Nt~U{16..128}'),
 }
 
 
@@ -63,6 +65,17 @@ def builder_for(name, kw):
     return lambda api, dtype='float32': fn(api, dtype=dtype, **kw)
 
 
+def sweep_builders(n_solves):
+    """One case builder per solve of the equation-discovery sweep (coefficients, grid sizes and
+    network seeds drawn as in cases.sweep_params)."""
+    import cases
+    out = []
+    for i, sp in enumerate(cases.sweep_params(n_solves)):
+        out.append(lambda api, dtype='float32', sp=sp, i=i:
+                   cases.sweep_ag(api, seed=1000 + i, dtype=dtype, **sp))
+    return out
+
+
 def full_kwargs(args):
     kw = dict(WORKLOADS[args.workload][1])
     if args.points_per_axis:
@@ -82,15 +95,19 @@ def cpu_baseline(args, max_seconds):
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
     kw = WORKLOADS[args.workload][2]
-    prob, net = O.build_problem(builder_for(args.workload, kw), 'float32')
-    n_pts = prob.points.shape[0]
-    opt = torch.optim.Adam(net.parameters(), lr=1e-3)
+    if args.workload == 'sweep':
+        built = [O.build_problem(b, 'float32') for b in sweep_builders(kw['n_solves'])]
+    else:
+        built = [O.build_problem(builder_for(args.workload, kw), 'float32')]
+    n_pts = sum(prob.points.shape[0] for prob, _ in built)
+    opts = [torch.optim.Adam(net.parameters(), lr=1e-3) for _, net in built]
 
     def step():
-        opt.zero_grad()
-        r = prob.evaluate(net)
-        r['loss'].backward()
-        opt.step()
+        for (prob, net), opt in zip(built, opts):
+            opt.zero_grad()
+            r = prob.evaluate(net)
+            r['loss'].backward()
+            opt.step()
     for _ in range(2):
         step()
     times = []
@@ -167,6 +184,87 @@ def read_traffic(tag):
         if ln.startswith('dram_bytes_per_point:'):
             return float(ln.split(':')[1])
     return None
+
+
+def run_sweep(args, world):
+    """256 solves of u_t = a u_xx + b u u_x + c u in one loss+gradient launch per step, one
+    batched Adam launch, against 256 separate solves on the CPU sample."""
+    import torch
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300 import _lib
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    n_solves = WORKLOADS['sweep'][1]['n_solves']
+    models = []
+    for b in sweep_builders(n_solves):
+        d, bc, eq, net, kw = b(T)
+        models.append(T.Model(net, d, eq, bc))
+    bm = T.BatchedModel(models)
+    bm.compile('autograd', lambda_operator=1, lambda_bound=1, precision=args.precision)
+    n_pts = sum(ir.n_residual_rows for ir in bm.irs)
+    flush = torch.empty(2 * L2_BYTES // 4, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    m = torch.zeros_like(bm.flat); v = torch.zeros_like(bm.flat); st = torch.zeros(1, device=dev)
+    hp = _lib.AdamDesc()
+    hp.lr, hp.beta1, hp.beta2, hp.eps = 1e-3, 0.9, 0.999, 1e-8
+    lib = _lib.load()
+
+    def step():
+        bm.plan.loss_grad(bm.flat, bm.grad, bm.loss, bm.outputs)
+        _lib.check(lib.tdg_adam_step(bm.flat.data_ptr(), bm.grad.data_ptr(), m.data_ptr(),
+                                     v.data_ptr(), st.data_ptr(), bm.flat.numel(), hp,
+                                     stream.cuda_stream), 'adam')
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    l0 = _lib.launch_count()
+    with ClockSampler(dev.index) as clk:
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
+    launches = _lib.launch_count() - l0
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    # end to end: host copies of every solve's points each step, loss read back
+    host = [t.cpu().pin_memory() for t in bm.plan.arrays]
+    t0 = time.perf_counter()
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(e2e_steps):
+        for h, d_ in zip(host, bm.plan.arrays):
+            d_.copy_(h, non_blocking=True)
+        bm.evaluate(with_grad=True)
+        _lib.check(lib.tdg_adam_step(bm.flat.data_ptr(), bm.grad.data_ptr(), m.data_ptr(),
+                                     v.data_ptr(), st.data_ptr(), bm.flat.numel(), hp,
+                                     stream.cuda_stream), 'adam')
+        bm.loss.cpu()
+    e2e_sec = (time.perf_counter() - t0) / e2e_steps
+    flops = bm.plan.info.flops_hidden
+    peaks_path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+    peak = peaks.get('bf16_tflops', 1900.0) / 2.0
+    achieved = flops / (ms / 1e3) / 1e12
+    return {'metric': METRIC, 'value': round(world * n_pts / (ms / 1e3), 1), 'unit': UNIT,
+            'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': round(ms, 4), 'steps_per_s': round(1e3 / ms, 3),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded coefficients, grids and networks)',
+            'config': {'workload': WORKLOADS['sweep'][3], 'solves': n_solves,
+                       'collocation_points': n_pts, 'precision': args.precision,
+                       'form': 'fused, one launch for all solves', 'optimizer': 'Adam lr=1e-3',
+                       'l2': 'flushed between timed steps (256 MiB write)',
+                       'parallelism': f'replicas x{world}'},
+            'e2e': {'value': round(world * n_pts / e2e_sec, 1), 'unit': UNIT,
+                    'h2d_bytes_per_step': sum(h.numel() * 4 for h in host),
+                    'd2h_bytes_per_step': bm.loss.numel() * 8},
+            'roofline': {'bound': 'tensor', 'achieved': round(achieved, 3), 'peak': round(peak, 1),
+                         'unit': 'TFLOP/s', 'frac': round(achieved / peak, 5), 'traffic': None,
+                         'kernel': 'fused loss+gradient (all solves) + Adam',
+                         'algorithmic_flops_per_launch': flops},
+            'gpu_launches': int(launches), 'clocks': clk.summary(), 'impl': 'ours'}
 
 
 def run_ours(args, rank, world):
@@ -303,7 +401,7 @@ def main():
     import torch
     if world > 1:
         torch.distributed.init_process_group('nccl')
-    line = run_ours(args, rank, world)
+    line = run_sweep(args, world) if args.workload == 'sweep' else run_ours(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline:
             line['cpu_baseline'] = {k: v for k, v in cpu_baseline(args, args.cpu_seconds).items()

@@ -1,0 +1,74 @@
+"""Model.train on the device path against the reference's own training run: 5 Adam(lr=1e-3)
+steps of train(epochs=6) (the reference performs epochs - 1 steps after an initial evaluate,
+tedeous/model.py:154-193). Covers the fused Adam kernel and the CUDA-graph replay of the step
+(steps 4 and 5 are replays)."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import build_model, golden, rel
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('name', ['heat_nn', 'burgers_ag', 'kdv_ag', 'kovasznay_ag'])
+def test_train_curve_and_weights_match_reference(name):
+    import torch_de_solver_gb300 as T
+    g = golden(name)
+    model = build_model(T, name, weights=g['weights'])
+    seen = []
+
+    class Record(T.Callback):
+        def on_epoch_end(self, logs=None):
+            seen.append(float(self.model.cur_loss.reshape(-1)[0]))
+
+    model.train(T.Optimizer('Adam', {'lr': 1e-3}), 6, callbacks=[Record()])
+    assert len(seen) == 5
+    assert rel(seen, g['curve32']) < 1e-5, (seen, g['curve32'])
+    w = torch.nn.utils.parameters_to_vector(model.net.parameters()).detach().cpu().numpy()
+    assert rel(w, g['final32']) < 1e-5, rel(w, g['final32'])
+
+
+@pytest.mark.gpu
+def test_train_with_lbfgs_closure():
+    """Optimizer("LBFGS") (LBFGS64, FP64 dots) through the reference closure: the loss decreases."""
+    import torch_de_solver_gb300 as T
+    g = golden('burgers_ag')
+    model = build_model(T, 'burgers_ag', weights=g['weights'])
+    l0 = model.solution_cls.evaluate()[0].item()
+    model.train(T.Optimizer('LBFGS', {'lr': 1e-1, 'max_iter': 5}), 3)
+    l1 = model.solution_cls.evaluate()[0].item()
+    assert l1 < l0
+
+
+@pytest.mark.gpu
+def test_lbfgs64_follows_torch_lbfgs():
+    """Same closure, same hyper-parameters: LBFGS64 (FP64 dots) and torch.optim.LBFGS (FP32 dots)
+    take the same steps up to dot-product rounding."""
+    import torch_de_solver_gb300 as T
+    g = golden('burgers_ag')
+    finals = []
+    for cls in (T.LBFGS64, torch.optim.LBFGS):
+        model = build_model(T, 'burgers_ag', weights=g['weights'])
+        opt = cls(model.net.parameters(), lr=0.5, max_iter=6, history_size=4)
+        sol = model.solution_cls
+
+        def closure():
+            opt.zero_grad()
+            loss, _ = sol.evaluate()
+            loss.backward()
+            return loss
+        for _ in range(3):
+            opt.step(closure)
+        finals.append(torch.nn.utils.parameters_to_vector(model.net.parameters()).detach().cpu().numpy())
+    assert rel(finals[0], finals[1]) < 1e-4, rel(finals[0], finals[1])
+
+
+@pytest.mark.gpu
+def test_dot_f64_exact_on_integers():
+    from torch_de_solver_gb300 import _lib
+    a = torch.arange(1, 100001, dtype=torch.float32, device='cuda')
+    out = torch.zeros(1, dtype=torch.float64, device='cuda')
+    _lib.check(_lib.load().tdg_dot_f64(a.data_ptr(), a.data_ptr(), a.numel(), out.data_ptr(),
+                                       torch.cuda.current_stream().cuda_stream), 'dot')
+    n = 100000
+    assert out.item() == n * (n + 1) * (2 * n + 1) / 6

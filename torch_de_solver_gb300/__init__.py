@@ -7,10 +7,10 @@ terms and parameter gradient run in hand-written sm_103a CUDA kernels (libtdg.so
 from .data import Conditions, Domain, Equation
 from .device import check_device, device_type, solver_device
 from .callbacks import Callback, CallbackList
-from .optimizer import FusedAdam, Optimizer
+from .optimizer import FusedAdam, LBFGS64, Optimizer
 from .solution import DevicePlan, Solution
-from .model import Model
+from .model import BatchedModel, Model
 
-__all__ = ['Domain', 'Conditions', 'Equation', 'Model', 'Optimizer', 'FusedAdam', 'Solution',
+__all__ = ['Domain', 'Conditions', 'Equation', 'Model', 'BatchedModel', 'Optimizer', 'FusedAdam', 'LBFGS64', 'Solution',
            'DevicePlan', 'Callback', 'CallbackList', 'solver_device', 'check_device',
            'device_type']

@@ -251,12 +251,22 @@ __device__ void jet_backward(const float* __restrict__ zbuf, float* __restrict__
   }
 }
 
+// Stage W [N x K] into shared memory. Vector loads need a 16-byte aligned W; the weights of
+// problem p start at p * n_params floats, which is not a multiple of 4 for odd parameter counts,
+// so misaligned layers are read element by element.
 __device__ void load_weights(float* __restrict__ wbuf, const float* __restrict__ W, int N, int K) {
-  const int K4 = K >> 2;
-  for (int e = threadIdx.x; e < N * K4; e += NT) {
-    const int n = e / K4, k = (e - n * K4) * 4;
-    *reinterpret_cast<float4*>(&wbuf[n * LDS + k]) =
-        __ldg(reinterpret_cast<const float4*>(&W[(int64_t)n * K + k]));
+  if ((reinterpret_cast<uintptr_t>(W) & 15) == 0) {
+    const int K4 = K >> 2;
+    for (int e = threadIdx.x; e < N * K4; e += NT) {
+      const int n = e / K4, k = (e - n * K4) * 4;
+      *reinterpret_cast<float4*>(&wbuf[n * LDS + k]) =
+          __ldg(reinterpret_cast<const float4*>(&W[(int64_t)n * K + k]));
+    }
+  } else {
+    for (int e = threadIdx.x; e < N * K; e += NT) {
+      const int n = e / K, k = e - n * K;
+      wbuf[n * LDS + k] = __ldg(&W[(int64_t)n * K + k]);
+    }
   }
 }
 

@@ -124,3 +124,95 @@ class Model:
         self._graph = None
         cbs.on_train_end()
         self._model_save(save_model, model_name)
+
+
+class BatchedModel:
+    """Many independent solves trained together: every solve keeps its own grid, boundary data,
+    equation coefficients and network, and one loss+gradient launch covers all of them (the tile
+    scheduler spreads their uneven point counts over the persistent CTAs). The networks must share
+    one shape; their parameters become views of one flat buffer [n_solves x P], so one fused Adam
+    launch updates all solves and the whole step is captured once in a CUDA graph. The reference
+    has no batched API: its equivalent is one Model per solve, trained one after another."""
+
+    def __init__(self, models: List[Model]):
+        if not models:
+            raise ValueError('no models')
+        self.models = list(models)
+
+    def compile(self, mode: str, lambda_operator, lambda_bound, h: float = 0.001,
+                inner_order: str = '1', boundary_order: str = '2', precision: str = 'fp32'):
+        from .prepare import lower
+        from .solution import DevicePlan, mlp_widths
+        if not torch.cuda.is_available():
+            raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
+        dev = torch.device('cuda', torch.cuda.current_device())
+        widths = mlp_widths(self.models[0].net)
+        irs = []
+        for m in self.models:
+            if mlp_widths(m.net) != widths:
+                raise ValueError('all networks of a batch must have the same shape')
+            grid = m.domain.build(mode=mode)
+            bconds = m.conditions.build(m.domain.variable_dict)
+            irs.append(lower(grid, m.equation.equation_lst, bconds, mode, lambda_operator,
+                             lambda_bound, h, inner_order, boundary_order, d_out=widths[-1]))
+        self.mode = mode
+        self.irs = irs
+        self.plan = DevicePlan(irs, widths, dev, precision)
+        P = self.plan.n_params
+        self.flat = torch.cat([torch.cat([p.detach().reshape(-1).float() for p in m.net.parameters()])
+                               for m in self.models]).to(dev)
+        with torch.no_grad():
+            for i, m in enumerate(self.models):
+                m.net.to(dev)
+                off = i * P
+                for p in m.net.parameters():
+                    n = p.numel()
+                    p.data = self.flat[off:off + n].view(p.shape)
+                    off += n
+        self.grad = torch.zeros_like(self.flat)
+        self.loss = torch.zeros(2 * len(self.models), dtype=torch.float64, device=dev)
+        self.outputs = torch.zeros(max(1, self.plan.n_outputs_total), device=dev)
+        self.device = dev
+        self._graph = None
+
+    def evaluate(self, with_grad: bool = False):
+        """Per-solve (loss, loss_normalized) as an (n_solves, 2) float64 tensor."""
+        if with_grad:
+            self.plan.loss_grad(self.flat, self.grad, self.loss, self.outputs)
+        else:
+            self.plan.loss(self.flat, self.loss, self.outputs)
+        return self.loss.view(-1, 2)
+
+    def train(self, lr: float = 1e-3, epochs: int = 1000, betas=(0.9, 0.999), eps: float = 1e-8,
+              use_graph: bool = True):
+        """Adam on every solve for epochs - 1 steps (the reference loop's count); returns the
+        per-solve losses seen by the last step."""
+        from . import _lib
+        m = torch.zeros_like(self.flat)
+        v = torch.zeros_like(self.flat)
+        step = torch.zeros(1, device=self.device)
+        hp = _lib.AdamDesc()
+        hp.lr, (hp.beta1, hp.beta2), hp.eps, hp.weight_decay, hp.maximize = lr, betas, eps, 0.0, 0
+        lib = _lib.load()
+
+        def one_step():
+            s = torch.cuda.current_stream(self.device)
+            self.plan.loss_grad(self.flat, self.grad, self.loss, self.outputs, stream=s)
+            _lib.check(lib.tdg_adam_step(self.flat.data_ptr(), self.grad.data_ptr(), m.data_ptr(),
+                                         v.data_ptr(), step.data_ptr(), self.flat.numel(), hp,
+                                         s.cuda_stream), 'tdg_adam_step')
+        self.evaluate()
+        graph = None
+        for t in range(1, epochs):
+            if graph is not None:
+                graph.replay()
+                continue
+            one_step()
+            if use_graph and t == 2:
+                cap = torch.cuda.Stream(self.device)
+                cap.wait_stream(torch.cuda.current_stream(self.device))
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph, stream=cap):
+                    one_step()
+        self._graph = graph
+        return self.loss.view(-1, 2).clone()

@@ -89,6 +89,119 @@ class FusedAdam(torch.optim.Optimizer):
         return loss
 
 
+class LBFGS64(torch.optim.Optimizer):
+    """L-BFGS with the step semantics of torch.optim.LBFGS (line_search_fn=None): lr, max_iter,
+    max_eval, tolerance_grad, tolerance_change, history_size; two-loop recursion over the stored
+    curvature pairs. Every dot product of the recursion and of the curvature test is accumulated in
+    FP64 on the device (tdg_dot_f64); vectors stay FP32 on the device."""
+
+    def __init__(self, params, lr=1.0, max_iter=20, max_eval=None, tolerance_grad=1e-7,
+                 tolerance_change=1e-9, history_size=100, line_search_fn=None):
+        if line_search_fn is not None:
+            raise NotImplementedError('LBFGS64 implements line_search_fn=None')
+        if max_eval is None:
+            max_eval = max_iter * 5 // 4
+        super().__init__(params, dict(lr=lr, max_iter=max_iter, max_eval=max_eval,
+                                      tolerance_grad=tolerance_grad,
+                                      tolerance_change=tolerance_change,
+                                      history_size=history_size))
+        if len(self.param_groups) != 1:
+            raise NotImplementedError('LBFGS64 takes one parameter group')
+        self._params = self.param_groups[0]['params']
+        dev = self._params[0].device
+        self._dot_out = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def _dot(self, a, b):
+        _lib.check(_lib.load().tdg_dot_f64(a.data_ptr(), b.data_ptr(), a.numel(),
+                                           self._dot_out.data_ptr(),
+                                           torch.cuda.current_stream(a.device).cuda_stream),
+                   'tdg_dot_f64')
+        return float(self._dot_out.item())
+
+    def _flat_grad(self):
+        return torch.cat([torch.zeros(p.numel(), device=p.device) if p.grad is None
+                          else p.grad.reshape(-1).to(torch.float32) for p in self._params])
+
+    def _add(self, t, d):
+        off = 0
+        for p in self._params:
+            n = p.numel()
+            p.add_(d[off:off + n].view_as(p), alpha=t)
+            off += n
+
+    @torch.no_grad()
+    def step(self, closure):
+        gr = self.param_groups[0]
+        lr, max_iter, max_eval = gr['lr'], gr['max_iter'], gr['max_eval']
+        tol_grad, tol_change, hist = gr['tolerance_grad'], gr['tolerance_change'], gr['history_size']
+        st = self.state[self._params[0]]
+        st.setdefault('func_evals', 0)
+        st.setdefault('n_iter', 0)
+        with torch.enable_grad():
+            orig_loss = closure()
+        loss = float(orig_loss)
+        evals = 1
+        st['func_evals'] += 1
+        g = self._flat_grad()
+        if float(g.abs().max()) <= tol_grad:
+            return orig_loss
+        d, t = st.get('d'), st.get('t')
+        dirs, stps, ro = st.get('old_dirs'), st.get('old_stps'), st.get('ro')
+        h_diag, g_prev, loss_prev = st.get('H_diag'), st.get('prev_flat_grad'), st.get('prev_loss')
+        n_iter = 0
+        while n_iter < max_iter:
+            n_iter += 1
+            st['n_iter'] += 1
+            if st['n_iter'] == 1:
+                d = g.neg()
+                dirs, stps, ro = [], [], []
+                h_diag = 1.0
+            else:
+                y = g - g_prev
+                s = d * t
+                ys = self._dot(y, s)
+                if ys > 1e-10:
+                    if len(dirs) == hist:
+                        dirs.pop(0), stps.pop(0), ro.pop(0)
+                    dirs.append(y)
+                    stps.append(s)
+                    ro.append(1.0 / ys)
+                    h_diag = ys / self._dot(y, y)
+                al = [0.0] * len(dirs)
+                q = g.neg()
+                for i in range(len(dirs) - 1, -1, -1):
+                    al[i] = self._dot(stps[i], q) * ro[i]
+                    q.add_(dirs[i], alpha=-al[i])
+                d = r = q * h_diag
+                for i in range(len(dirs)):
+                    be = self._dot(dirs[i], r) * ro[i]
+                    r.add_(stps[i], alpha=al[i] - be)
+            g_prev = g.clone()
+            loss_prev = loss
+            t = min(1.0, 1.0 / float(g.abs().sum())) * lr if st['n_iter'] == 1 else lr
+            gtd = self._dot(g, d)
+            if gtd > -tol_change:
+                break
+            ls_evals = 0
+            self._add(t, d)
+            if n_iter != max_iter:
+                with torch.enable_grad():
+                    loss = float(closure().detach())
+                g = self._flat_grad()
+                ls_evals = 1
+            evals += ls_evals
+            st['func_evals'] += ls_evals
+            if n_iter == max_iter or evals >= max_eval:
+                break
+            if float(g.abs().max()) <= tol_grad:
+                break
+            if float((d * t).abs().max()) <= tol_change or abs(loss - loss_prev) < tol_change:
+                break
+        st.update(d=d, t=t, old_dirs=dirs, old_stps=stps, ro=ro, H_diag=h_diag,
+                  prev_flat_grad=g_prev, prev_loss=loss_prev)
+        return orig_loss
+
+
 class Optimizer:
     """Name + hyper-parameters -> optimizer instance (tedeous/optimizers/optimizer.py:11-73)."""
 
@@ -111,6 +224,8 @@ class Optimizer:
             raise NotImplementedError(f'mode {mode!r}')
         if self.optimizer == 'Adam':
             opt = FusedAdam(model.parameters(), **self.params)
+        elif self.optimizer == 'LBFGS' and self.params.get('line_search_fn') is None:
+            opt = LBFGS64(model.parameters(), **self.params)
         else:
             opt = names[self.optimizer](model.parameters(), **self.params)
         if self.gamma is not None:
