@@ -54,6 +54,7 @@ def parse():
     ap.add_argument('--workload', default='kovasznay', choices=sorted(WORKLOADS))
     ap.add_argument('--points-per-axis', type=int, default=None)
     ap.add_argument('--precision', default='fp32')
+    ap.add_argument('--form', default='fused', choices=['fused', 'plain'])
     ap.add_argument('--cpu-seconds', type=float, default=20.0)
     ap.add_argument('--no-cpu-baseline', action='store_true')
     return ap.parse_args()
@@ -278,7 +279,7 @@ def run_ours(args, rank, world):
     domain, bnd, eq, net, ckw = builder_for(args.workload, kw)(T)
     ckw = dict(ckw)
     model = T.Model(net, domain, eq, bnd)
-    model.compile(ckw.pop('mode'), precision=args.precision, **ckw)
+    model.compile(ckw.pop('mode'), precision=args.precision, form=args.form, **ckw)
     sol = model.solution_cls
     plan = sol.plan
     n_pts = sol.ir.n_residual_rows
@@ -352,12 +353,14 @@ def run_ours(args, rank, world):
     kern_s = statistics.mean(kern_ms) / 1e3
     achieved = flops / kern_s / 1e12
     peak = bf16 / 2.0   # dense TF32 tensor rate = half the measured dense BF16 rate
-    tag = f'fused_fp32_{args.workload}'
+    tag = f'{args.form}_{args.precision}_{args.workload}'
     tpp = read_traffic(tag)
     roofline = {'bound': 'tensor', 'achieved': round(achieved, 3), 'peak': round(peak, 1),
                 'unit': 'TFLOP/s', 'frac': round(achieved / peak, 5),
                 'traffic': None if tpp is None else int(tpp * n_pts),
-                'kernel': 'tdg::fused_fp32_kernel (+ loss/gradient reductions)',
+                'kernel': ('tdg::fused_fp32_kernel' if args.precision == 'fp32' else
+                           'tdg::fused_tc_kernel (tcgen05)') + ' + reductions'
+                if args.form == 'fused' else 'plain form: all per-layer launches of the step',
                 'kernel_ms': round(statistics.mean(kern_ms), 4),
                 'algorithmic_flops_per_launch': flops,
                 'peak_source': 'MEASURED_PEAKS.json bf16_tflops / 2 (dense TF32 = half of BF16)'
@@ -368,7 +371,7 @@ def run_ours(args, rank, world):
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic (seeded grid, closed-form boundary data, seeded torch init)',
             'config': {'workload': WORKLOADS[args.workload][3], 'collocation_points': n_pts,
-                       'params': plan.n_params, 'precision': args.precision, 'form': 'fused',
+                       'params': plan.n_params, 'precision': args.precision, 'form': args.form,
                        'optimizer': 'Adam lr=1e-3',
                        'l2': 'flushed between timed steps (256 MiB write)',
                        'parallelism': f'replicas x{world}'},

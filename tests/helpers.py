@@ -18,7 +18,8 @@ def set_flat_weights(net, w):
                                         net.parameters())
 
 
-def build_model(api, name=None, builder=None, weights=None, precision='fp32', **case_kw):
+def build_model(api, name=None, builder=None, weights=None, precision='fp32', form='fused',
+                **case_kw):
     builder = builder or cases.GOLDEN_CASES[name]
     domain, bnd, eq, net, kw = builder(api, **case_kw) if case_kw else builder(api)
     if weights is not None:
@@ -26,7 +27,7 @@ def build_model(api, name=None, builder=None, weights=None, precision='fp32', **
     model = api.Model(net, domain, eq, bnd)
     kw = dict(kw)
     mode = kw.pop('mode')
-    model.compile(mode, precision=precision, **kw)
+    model.compile(mode, precision=precision, form=form, **kw)
     return model
 
 

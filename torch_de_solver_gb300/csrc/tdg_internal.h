@@ -115,6 +115,39 @@ struct TcLaunch {
   int* err;
 };
 size_t fused_tc_smem_bytes();
+
+// plain form: one launch per layer operation, activations of every row kept in device memory
+struct HostGroupInfo {
+  int64_t n_rows;
+  int32_t S, problem;
+};
+struct PlainArgs {
+  const DevGroup* groups;           // device
+  const HostGroupInfo* ginfo;       // host
+  int32_t n_groups;
+  const float* const* arrays;
+  const float* params;
+  float* grad;
+  int64_t n_params;
+  int32_t n_problems;
+  int32_t n_layers;
+  int32_t width[TDG_MAX_LAYERS + 1];
+  int64_t w_off[TDG_MAX_LAYERS], b_off[TDG_MAX_LAYERS];
+  float* act;                       // Z_l and H_l of every hidden layer of one group
+  float* g0;
+  float* g1;                        // dL/dH and dL/dZ ping-pong
+  float* y;
+  float* gy;                        // MLP outputs and their seeds
+  double* slot_sum;
+  int32_t n_slots;
+  const int32_t* slot_problem;
+  const double* slot_w;
+  const double* slot_wn;
+  double* loss;
+  float* outputs;
+  int32_t do_grad;
+};
+cudaError_t run_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
 cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
                                const int32_t* seg_list, int n_problems, int64_t n_params,

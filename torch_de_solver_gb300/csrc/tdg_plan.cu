@@ -73,6 +73,14 @@ struct tdg_plan {
   float* d_scratch = nullptr;
   unsigned char* d_wpack = nullptr;
   int* d_err = nullptr;
+  // plain form
+  std::vector<HostGroupInfo> ginfo;
+  float* d_act = nullptr;
+  float* d_g0 = nullptr;
+  float* d_g1 = nullptr;
+  float* d_y = nullptr;
+  float* d_gy = nullptr;
+  double* d_slot_sum = nullptr;
   int64_t wpack_fwd[TDG_MAX_LAYERS] = {0}, wpack_bwd[TDG_MAX_LAYERS] = {0};
   int64_t workspace_bytes = 0;
   bool arrays_dirty = false;
@@ -127,7 +135,8 @@ tdg_status dev_alloc(tdg_plan* p, void** dst, size_t bytes) {
 void free_plan(tdg_plan* p) {
   void* ptrs[] = {p->d_groups, p->d_tiles, p->d_cta_begin, (void*)p->d_arrays, p->d_seg_begin,
                   p->d_seg_list, p->d_partial, p->d_slot_partial, p->d_slot_problem,
-                  p->d_slot_w, p->d_slot_wn, p->d_scratch, p->d_wpack, p->d_err};
+                  p->d_slot_w, p->d_slot_wn, p->d_scratch, p->d_wpack, p->d_err,
+                  p->d_act, p->d_g0, p->d_g1, p->d_y, p->d_gy, p->d_slot_sum};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -329,7 +338,9 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
   }
   if (d.precision != TDG_PREC_FP32 && d.precision != TDG_PREC_TF32 && d.precision != TDG_PREC_BF16)
     return fail(TDG_ERR_UNSUPPORTED, "precision %d not built", d.precision);
-  if (d.form != TDG_FORM_FUSED) return fail(TDG_ERR_UNSUPPORTED, "form %d not built", d.form);
+  if (d.form != TDG_FORM_FUSED && d.form != TDG_FORM_PLAIN) return fail(TDG_ERR_UNSUPPORTED, "form %d not built", d.form);
+  if (d.form == TDG_FORM_PLAIN && d.precision != TDG_PREC_FP32)
+    return fail(TDG_ERR_UNSUPPORTED, "the plain form computes in FP32 only");
   if (d.n_problems < 1) return fail(TDG_ERR_INVALID, "n_problems < 1");
   if (d.n_groups < 1) return fail(TDG_ERR_INVALID, "no groups");
   if (d.n_slots < 1 || d.n_slots > MAX_SLOTS) return fail(TDG_ERR_UNSUPPORTED, "%d loss slots (1..%d)", d.n_slots, MAX_SLOTS);
@@ -370,6 +381,7 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     tdg_status st = build_group(d, g, d_in, d_out, groups[gi], S);
     if (st != TDG_OK) { free_plan(p); return st; }
     p->max_streams = std::max(p->max_streams, S);
+    p->ginfo.push_back(HostGroupInfo{g.n_rows, S, g.problem});
     const int T = RMAX / S;
     for (int r0 = 0; r0 < g.n_rows; r0 += T)
       tiles.push_back(DevTile{gi, r0, std::min(T, g.n_rows - r0), 0, 0, {0, 0, 0}});
@@ -438,6 +450,20 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     return st;
   }
   if (cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) { free_plan(p); return fail(TDG_ERR_CUDA, "cudaMemset"); }
+  if (d.form == TDG_FORM_PLAIN) {
+    int64_t rows_max = 0, wsum = 0, wmax = 0;
+    for (auto& gi : p->ginfo) rows_max = std::max<int64_t>(rows_max, gi.n_rows * gi.S);
+    for (int l = 1; l < L; ++l) { wsum += 2 * d.mlp.width[l]; wmax = std::max<int64_t>(wmax, d.mlp.width[l]); }
+    if ((st = dev_alloc(p, (void**)&p->d_act, sizeof(float) * rows_max * wsum)) ||
+        (st = dev_alloc(p, (void**)&p->d_g0, sizeof(float) * rows_max * wmax)) ||
+        (st = dev_alloc(p, (void**)&p->d_g1, sizeof(float) * rows_max * wmax)) ||
+        (st = dev_alloc(p, (void**)&p->d_y, sizeof(float) * rows_max * d_out)) ||
+        (st = dev_alloc(p, (void**)&p->d_gy, sizeof(float) * rows_max * d_out)) ||
+        (st = dev_alloc(p, (void**)&p->d_slot_sum, sizeof(double) * d.n_slots))) {
+      free_plan(p);
+      return st;
+    }
+  }
   if (d.precision != TDG_PREC_FP32) {
     // packed hidden weights for the tensor-core kernel: forward and transposed operand per layer
     const int es = d.precision == TDG_PREC_BF16 ? 2 : 4;
@@ -508,6 +534,32 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
   for (int l = 0; l <= p->n_layers; ++l) a.width[l] = p->width[l];
   for (int l = 0; l < p->n_layers; ++l) { a.w_off[l] = p->w_off[l]; a.b_off[l] = p->b_off[l]; }
   cudaError_t e;
+  if (p->form == TDG_FORM_PLAIN) {
+    PlainArgs pa{};
+    pa.groups = p->d_groups;
+    pa.ginfo = p->ginfo.data();
+    pa.n_groups = (int)p->ginfo.size();
+    pa.arrays = p->d_arrays;
+    pa.params = params;
+    pa.grad = grad;
+    pa.n_params = p->n_params;
+    pa.n_problems = p->n_problems;
+    pa.n_layers = p->n_layers;
+    for (int l = 0; l <= p->n_layers; ++l) pa.width[l] = p->width[l];
+    for (int l = 0; l < p->n_layers; ++l) { pa.w_off[l] = p->w_off[l]; pa.b_off[l] = p->b_off[l]; }
+    pa.act = p->d_act; pa.g0 = p->d_g0; pa.g1 = p->d_g1; pa.y = p->d_y; pa.gy = p->d_gy;
+    pa.slot_sum = p->d_slot_sum;
+    pa.n_slots = p->n_slots;
+    pa.slot_problem = p->d_slot_problem;
+    pa.slot_w = p->d_slot_w;
+    pa.slot_wn = p->d_slot_wn;
+    pa.loss = loss;
+    pa.outputs = outputs;
+    pa.do_grad = do_grad ? 1 : 0;
+    e = run_plain(pa, s);
+    if (e != cudaSuccess) return cuda_fail(e, "plain form launch");
+    return TDG_OK;
+  }
   if (p->precision == TDG_PREC_FP32) {
     e = launch_fused_fp32(a, p->n_ctas, s);
   } else {
