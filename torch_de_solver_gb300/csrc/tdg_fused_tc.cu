@@ -46,21 +46,31 @@ __device__ __forceinline__ float dpowf_(float x, float p) {
   return p * powf(x, p - 1.f);
 }
 
-struct Sig {   // tanh and its derivatives for 4 neurons
-  float t[4], s1[4], s2[4], s3[4], s4[4];
+__device__ __forceinline__ float4 f4mul(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 f4scale(float4 a, float c) { return make_float4(a.x * c, a.y * c, a.z * c, a.w * c); }
+
+struct Sig {   // tanh and its derivatives, as functions of t = tanh(z), for 4 neurons
+  float4 t, s1, s2, s3, s4;
   __device__ __forceinline__ void make(const float4 z, bool need4) {
-    const float zz[4] = {z.x, z.y, z.z, z.w};
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      t[i] = tanhf(zz[i]);
-      s1[i] = 1.f - t[i] * t[i];
-      s2[i] = -2.f * t[i] * s1[i];
-      s3[i] = s1[i] * (6.f * t[i] * t[i] - 2.f);
-      s4[i] = need4 ? t[i] * s1[i] * (16.f - 24.f * t[i] * t[i]) : 0.f;
-    }
+    t = make_float4(tanhf(z.x), tanhf(z.y), tanhf(z.z), tanhf(z.w));
+    const float4 tt = f4mul(t, t);
+    s1 = make_float4(1.f - tt.x, 1.f - tt.y, 1.f - tt.z, 1.f - tt.w);
+    s2 = f4scale(f4mul(t, s1), -2.f);
+    s3 = f4mul(s1, make_float4(6.f * tt.x - 2.f, 6.f * tt.y - 2.f, 6.f * tt.z - 2.f, 6.f * tt.w - 2.f));
+    s4 = need4 ? f4mul(f4mul(t, s1), make_float4(16.f - 24.f * tt.x, 16.f - 24.f * tt.y,
+                                                  16.f - 24.f * tt.z, 16.f - 24.f * tt.w))
+               : make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  __device__ __forceinline__ float at(int k, int i) const {
-    return sk(k, t[i], s1[i], s2[i], s3[i], s4[i]);
+  // the k-th derivative; k is the same for every thread of a group's table entry (uniform branch)
+  __device__ __forceinline__ float4 sel(int k) const {
+    switch (k) {
+      case 0: return t;
+      case 1: return s1;
+      case 2: return s2;
+      case 3: return s3;
+      default: return s4;
+    }
   }
 };
 
@@ -131,11 +141,12 @@ __device__ __forceinline__ void gemm_issue(uint32_t d, const unsigned char* a, c
   commit(bar);
 }
 
-// thread (p, 4 neurons): tanh jet of every stream of point p from plain Z rows, written as
-// operand rows (or, if `plain_out`, as unrounded FP32 in the TF32 operand layout).
+// thread (p, 4 neurons): tanh jet of every stream of point p from plain Z rows in P, written as
+// operand rows of `out`, or, when `inplace`, back into P as FP32 rows (streams of a site from the
+// highest order down, the value stream last, so every Z a rule reads is still intact).
 template <bool BF16>
-__device__ void jet_fwd_rows(const float* __restrict__ P, unsigned char* __restrict__ out,
-                             const DevGroup& G, int np, bool plain_out) {
+__device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ out,
+                             const DevGroup& G, int np, bool inplace) {
   const int T = G.T;
   const int n4s = np >> 2;
   for (int e = threadIdx.x; e < T * n4s; e += NTC) {
@@ -145,29 +156,20 @@ __device__ void jet_fwd_rows(const float* __restrict__ P, unsigned char* __restr
       const int base = G.site_streams[q][0];
       Sig sg;
       sg.make(ld4(&P[(base * T + p) * LDS + n]), false);
-      for (int m = 0; m < ns; ++m) {
+      for (int m = ns - 1; m >= 0; --m) {
         const int s = G.site_streams[q][m];
-        float h[4] = {0.f, 0.f, 0.f, 0.f};
-        if (m == 0) {
-#pragma unroll
-          for (int i = 0; i < 4; ++i) h[i] = sg.t[i];
-        } else {
+        float4 h = sg.t;
+        if (m > 0) {
+          h = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int u = 0; u < G.st_nrule[s]; ++u) {
             const DevRule& ru = G.rules[s][u];
-            float v[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) v[i] = (float)ru.mult * sg.at(ru.k, i);
-            for (int f = 0; f < ru.k; ++f) {
-              const float4 z = ld4(&P[(ru.sub[f] * T + p) * LDS + n]);
-              v[0] *= z.x; v[1] *= z.y; v[2] *= z.z; v[3] *= z.w;
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i) h[i] += v[i];
+            float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
+            for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4(&P[(ru.sub[f] * T + p) * LDS + n]));
+            h = f4add(h, v);
           }
         }
-        const float4 hv = make_float4(h[0], h[1], h[2], h[3]);
-        if (plain_out) *reinterpret_cast<float4*>(out + ofs(s * T + p, n, np, 4)) = hv;
-        else put4<BF16>(out, s * T + p, n, np, hv);
+        if (inplace) st4(&P[(s * T + p) * LDS + n], h);
+        else put4<BF16>(out, s * T + p, n, np, h);
       }
     }
   }
@@ -306,8 +308,12 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
     }
     __syncthreads();
-    jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), L == 2);
-    zero_rows<BF16>(opA, R, p16(A.width[1]), L == 2 ? 4 : ES);
+    if (L == 2) {
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true);   // last hidden layer: FP32 rows in P1
+    } else {
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), false);
+      zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
+    }
     cx.publish();
 
     // ---- hidden layers on the tensor cores
@@ -341,23 +347,26 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
       fence_before();
       __syncthreads();
-      const bool last = j == L - 2;
-      jet_fwd_rows<BF16>(P1, opA, G, np, last);
-      zero_rows<BF16>(opA, R, np, last ? 4 : ES);
+      if (j == L - 2) {
+        jet_fwd_rows<BF16>(P1, opA, G, np, true);   // last hidden layer: FP32 rows in P1
+      } else {
+        jet_fwd_rows<BF16>(P1, opA, G, np, false);
+        zero_rows<BF16>(opA, R, np, ES);
+      }
       cx.publish();
     }
 
-    // ---- output layer (H_{L-1} in opA as FP32, TF32 layout)
+    // ---- output layer (H_{L-1} as FP32 rows in P1)
     {
-      const int K = A.width[L - 1], kp = p16(K);
+      const int K = A.width[L - 1];
       const float* Wl = prm + A.w_off[L - 1];
       const float* bl = prm + A.b_off[L - 1];
       for (int e = tid; e < RMAX * d_out; e += NTC) {
-        const int r = e / d_out, o = e - r * d_out;
+        const int r = e % RMAX, o = e / RMAX;
         float z = 0.f;
         const float* w = &Wl[(int64_t)o * K];
         for (int k = 0; k < K; k += 4) {
-          const float4 hv = ld4o(opA, ofs(r, k, kp, 4));
+          const float4 hv = ld4(&P1[r * LDS + k]);
           z = fmaf(hv.x, __ldg(&w[k]), z);
           z = fmaf(hv.y, __ldg(&w[k + 1]), z);
           z = fmaf(hv.z, __ldg(&w[k + 2]), z);
@@ -370,19 +379,19 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     }
     __syncthreads();
 
-    // ---- operator program, squared error, seeds, program adjoint (one thread per point)
+    // ---- operator program: term values per (point, term), outputs and squared errors per
+    // (point, output), the loss seeds, then the program adjoint per (point, term). Scratch lives in
+    // opB, which no MMA reads between the last forward GEMM and the first backward bulk copy.
     const int n_out = G.n_outputs;
-    float err2[MAX_OUT];
-#pragma unroll
-    for (int o = 0; o < MAX_OUT; ++o) err2[o] = 0.f;
-    if (tid < T) {
-      const int p = tid;
-      const bool valid = p < nvalid;
-      float outv[MAX_OUT];
-#pragma unroll
-      for (int o = 0; o < MAX_OUT; ++o) outv[o] = 0.f;
-      for (int t = 0; t < G.n_terms; ++t) {
+    {
+      float* tv = reinterpret_cast<float*>(opB);           // [MAX_TERMS][T] term values
+      float* seedv = tv + MAX_TERMS * RMAX;                 // [MAX_OUT][T] dL/d(output)
+      double* e2 = reinterpret_cast<double*>(seedv + MAX_OUT * RMAX);   // [MAX_OUT][T]
+      const int nt = G.n_terms;
+      for (int e = tid; e < T * nt; e += NTC) {
+        const int p = e % T, t = e / T;
         const DevTerm& tm = G.terms[t];
+        const bool valid = p < nvalid;
         const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
         float prod = 1.f;
         for (int f = 0; f < tm.n_factors; ++f) {
@@ -394,25 +403,36 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           }
           prod *= powf_(F, fc.power);
         }
-        outv[tm.output] += c * prod;
+        tv[t * RMAX + p] = c * prod;
       }
-      float seed[MAX_OUT];
-#pragma unroll
-      for (int o = 0; o < MAX_OUT; ++o) seed[o] = 0.f;
-      for (int o = 0; o < n_out; ++o) {
+      __syncthreads();
+      for (int e = tid; e < T * n_out; e += NTC) {
+        const int p = e % T, o = e / T;
+        const bool valid = p < nvalid;
+        float out = 0.f;
+        for (int t = 0; t < nt; ++t)
+          if (G.terms[t].output == o) out += tv[t * RMAX + p];
         const float tgt = (G.target_array >= 0 && valid)
                               ? A.arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
-        const float e = valid ? outv[o] - tgt : 0.f;
-        err2[o] = e * e;
-        seed[o] = e * G.seed_scale[o];
+        const float err = valid ? out - tgt : 0.f;
+        e2[o * RMAX + p] = (double)err * (double)err;
+        seedv[o * RMAX + p] = err * G.seed_scale[o];
         if (A.outputs && G.out_offset >= 0 && valid)
-          A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = outv[o];
+          A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = out;
+      }
+      __syncthreads();
+      if (tid < n_out) {   // fixed-order FP64 sum over the tile's points
+        double sum = 0.0;
+        for (int p = 0; p < T; ++p) sum += e2[tid * RMAX + p];
+        cur_slot[tid] += sum;
       }
       if (A.do_grad) {
-        for (int t = 0; t < G.n_terms; ++t) {
+        for (int e = tid; e < T * nt; e += NTC) {
+          const int p = e % T, t = e / T;
           const DevTerm& tm = G.terms[t];
+          const bool valid = p < nvalid;
           const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
-          const float dt = seed[tm.output] * c;
+          const float dt = seedv[tm.output * RMAX + p] * c;
           if (dt == 0.f) continue;
           float F[MAX_TERM_FACTORS];
           for (int f = 0; f < tm.n_factors; ++f) {
@@ -431,24 +451,10 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
               if (g != f) d *= powf_(F[g], G.factors[tm.factor_first + g].power);
             for (int u = 0; u < fc.n_parts; ++u) {
               const DevPart& pt = G.parts[fc.part_first + u];
-              gybuf[(pt.stream * T + p) * MAX_OUT + fc.var] += d * pt.weight;
+              atomicAdd(&gybuf[(pt.stream * T + p) * MAX_OUT + fc.var], d * pt.weight);
             }
           }
         }
-      }
-    }
-    {
-      for (int o = 0; o < n_out; ++o) {
-        double v = (double)err2[o];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if (lane == 0) wred[warp * MAX_OUT + o] = v;
-      }
-      __syncthreads();
-      if (tid < n_out) {
-        double s = 0.0;
-        for (int w = 0; w < NTC / 32; ++w) s += wred[w * MAX_OUT + tid];
-        cur_slot[tid] += s;
       }
     }
     if (!A.do_grad) continue;
@@ -456,7 +462,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
 
     float* grad = A.partial + (int64_t)tile.seg * A.part_stride;
     const bool first = tile.first_in_seg != 0;
-    // ---- output layer backward: dW, db; dL/dH_{L-1} -> P1
+    // ---- output layer backward: dW, db (H_{L-1} in P1), then dL/dH_{L-1} -> P1
     {
       const int K = A.width[L - 1], kp = p16(K);
       const float* Wl = prm + A.w_off[L - 1];
@@ -464,16 +470,17 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       float* db = grad + A.b_off[L - 1];
       for (int e = tid; e < d_out * K; e += NTC) {
         const int o = e / K, k = e - o * K;
-        float s = 0.f;
-        for (int r = 0; r < R; ++r) s = fmaf(gybuf[r * MAX_OUT + o], get<false>(opA, ofs(r, k, kp, 4)), s);
-        dW[(int64_t)o * K + k] = first ? s : dW[(int64_t)o * K + k] + s;
+        float sum = 0.f;
+        for (int r = 0; r < R; ++r) sum = fmaf(gybuf[r * MAX_OUT + o], P1[r * LDS + k], sum);
+        dW[(int64_t)o * K + k] = first ? sum : dW[(int64_t)o * K + k] + sum;
       }
       for (int o = tid; o < d_out; o += NTC) {
-        float s = 0.f;
+        float sum = 0.f;
         for (int r = 0; r < R; ++r)
-          if (row_v[r]) s += gybuf[r * MAX_OUT + o];
-        db[o] = first ? s : db[o] + s;
+          if (row_v[r]) sum += gybuf[r * MAX_OUT + o];
+        db[o] = first ? sum : db[o] + sum;
       }
+      __syncthreads();
       for (int e = tid; e < RMAX * (kp >> 2); e += NTC) {
         const int r = e % RMAX, k = (e / RMAX) * 4;
         float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -487,8 +494,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         st4(&P1[r * LDS + k], make_float4(v[0], v[1], v[2], v[3]));
       }
     }
-    fence_before();
-    __syncthreads();
+    cx.publish();   // the program's scratch in opB is overwritten by the next bulk copy
 
     for (int l = L - 1; l >= 1; --l) {
       const int N = A.width[l], np = p16(N);
@@ -509,22 +515,16 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             sg.make(ld4o(opB, ofs(base * T + p, n, np, 4)), true);
             for (int m = 0; m < ns; ++m) {
               const int b = G.site_streams[q][m];
-              float acc[4] = {0.f, 0.f, 0.f, 0.f};
+              float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
               const int pf = G.st_pull_first[b];
               for (int u = 0; u < G.st_npull[b]; ++u) {
                 const DevPull& pl = G.pulls[pf + u];
-                const float4 g = ld4(&P1[(pl.alpha * T + p) * LDS + n]);
-                float v[4] = {g.x, g.y, g.z, g.w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i) v[i] *= (float)pl.mult * sg.at(pl.kk, i);
-                for (int f = 0; f < pl.n_oth; ++f) {
-                  const float4 z = ld4o(opB, ofs(pl.oth[f] * T + p, n, np, 4));
-                  v[0] *= z.x; v[1] *= z.y; v[2] *= z.z; v[3] *= z.w;
-                }
-#pragma unroll
-                for (int i = 0; i < 4; ++i) acc[i] += v[i];
+                float4 v = f4mul(ld4(&P1[(pl.alpha * T + p) * LDS + n]),
+                                 f4scale(sg.sel(pl.kk), (float)pl.mult));
+                for (int f = 0; f < pl.n_oth; ++f) v = f4mul(v, ld4o(opB, ofs(pl.oth[f] * T + p, n, np, 4)));
+                acc = f4add(acc, v);
               }
-              const float4 gz = make_float4(acc[0], acc[1], acc[2], acc[3]);
+              const float4 gz = acc;
               st4(&P1[(b * T + p) * LDS + n], gz);
               if (l >= 2) put4<BF16>(opA, b * T + p, n, np, gz);
             }
@@ -607,30 +607,40 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       // Z_{l-1} (scratch slot l-2, interleaved FP32) -> P1 region by bulk copy
       unsigned char* zst = reinterpret_cast<unsigned char*>(P1);
       cx.load(zst, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));
-      // H_{l-1}^T [kp x 128 rows] -> opB: thread (neuron n, 4 consecutive rows)
-      for (int e = tid; e < kp * 32; e += NTC) {
-        const int n = e % kp, r4 = (e / kp) * 4;
-        float h[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int i = 0; i < 4; ++i) {
-          const int r = r4 + i;
-          const int sr = row_s[r];
-          if (sr < 0) continue;
+      // H_{l-1}^T [kp x 128 rows] -> opB. Lanes take consecutive rows (conflict-free reads of the
+      // interleaved Z), 4 neurons each; each quad of lanes then transposes its 4 x 4 block with
+      // shuffles so that a lane stores one neuron for 4 consecutive rows.
+      for (int e = tid; e < 32 * kp; e += NTC) {
+        const int r = e & 127, n = (e >> 7) * 4;
+        float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int sr = row_s[r];
+        if (sr >= 0) {
           const int p = row_p[r];
           const int q = G.st_site[sr];
-          const float z0 = get<false>(zst, ofs(G.site_streams[q][0] * T + p, n, kp, 4));
-          const float t = tanhf(z0);
-          if (G.st_order[sr] == 0) { h[i] = t; continue; }
-          const float s1 = 1.f - t * t, s2 = -2.f * t * s1, s3 = s1 * (6.f * t * t - 2.f);
-          float acc = 0.f;
-          for (int u = 0; u < G.st_nrule[sr]; ++u) {
-            const DevRule& ru = G.rules[sr][u];
-            float v = (float)ru.mult * sk(ru.k, t, s1, s2, s3, 0.f);
-            for (int f = 0; f < ru.k; ++f) v *= get<false>(zst, ofs(ru.sub[f] * T + p, n, kp, 4));
-            acc += v;
+          Sig sg;
+          sg.make(ld4o(zst, ofs(G.site_streams[q][0] * T + p, n, kp, 4)), false);
+          if (G.st_order[sr] == 0) {
+            h = sg.t;
+          } else {
+            for (int u = 0; u < G.st_nrule[sr]; ++u) {
+              const DevRule& ru = G.rules[sr][u];
+              float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
+              for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4o(zst, ofs(ru.sub[f] * T + p, n, kp, 4)));
+              h = f4add(h, v);
+            }
           }
-          h[i] = acc;
         }
-        put4<BF16>(opB, n, r4, 128, make_float4(h[0], h[1], h[2], h[3]));
+        const int qd = lane & 3, qbase = lane & ~3;
+        float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int si = (qd - k) & 3;
+          const float send = si == 0 ? h.x : si == 1 ? h.y : si == 2 ? h.z : h.w;
+          const float got = __shfl_sync(0xffffffffu, send, qbase | ((qd + k) & 3));
+          const int di = (qd + k) & 3;
+          if (di == 0) o0 = got; else if (di == 1) o1 = got; else if (di == 2) o2 = got; else o3 = got;
+        }
+        put4<BF16>(opB, n + qd, r & ~3, 128, make_float4(o0, o1, o2, o3));
       }
       cx.publish();
       // dW: D2[128 x kp] = A[128 x 128] . B[kp x 128]^T
