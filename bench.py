@@ -53,7 +53,7 @@ def parse():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--workload', default='kovasznay', choices=sorted(WORKLOADS))
     ap.add_argument('--points-per-axis', type=int, default=None)
-    ap.add_argument('--precision', default='fp32')
+    ap.add_argument('--precision', default='3xtf32', choices=['fp32', '3xtf32', 'tf32', 'bf16'])
     ap.add_argument('--form', default='fused', choices=['fused', 'plain'])
     ap.add_argument('--cpu-seconds', type=float, default=20.0)
     ap.add_argument('--no-cpu-baseline', action='store_true')

@@ -141,12 +141,42 @@ __device__ __forceinline__ void gemm_issue(uint32_t d, const unsigned char* a, c
   commit(bar);
 }
 
+// Split TF32: D = A . B^T as hi*hi + hi*lo + lo*hi, FP32 accumulate. A hi in shared memory (k
+// elements per row, rounded), A lo in tensor memory (columns), B streamed from global memory in
+// two K-halves of [hi | lo] blocks through opB. All threads call this (it waits on the copies and
+// the MMAs); thread 0 issues.
+__device__ void gemm3x(TcCtx& cx, uint32_t d, const unsigned char* a, uint32_t a_lo, unsigned char* opB,
+                       const unsigned char* b_src, int n, int k) {
+  const uint32_t idesc = instr_desc<false>(128, n);
+  const int kh = k / 2;
+  const uint32_t half_bytes = (uint32_t)n * kh * 4;
+  const uint32_t sbo_a = (uint32_t)(k / 4) * 128, sbo_b = (uint32_t)(kh / 4) * 128;
+  for (int h = 0; h < 2; ++h) {
+    cx.load(opB, b_src + (size_t)h * 2 * half_bytes, 2 * half_bytes);
+    if (threadIdx.x == 0) {
+      fence_after();
+      const uint32_t a0 = smem_u32(a), b0 = smem_u32(opB);
+      for (int j = 0; j < kh / 8; ++j) {
+        const int kk = h * kh + 8 * j;
+        const uint64_t ad = smem_desc(a0 + (kk / 8) * 256, 128, sbo_a);
+        const uint64_t bh = smem_desc(b0 + j * 256, 128, sbo_b);
+        const uint64_t bl = smem_desc(b0 + half_bytes + j * 256, 128, sbo_b);
+        mma<false>(d, ad, bh, idesc, h > 0 || j > 0);
+        mma<false>(d, ad, bl, idesc, true);
+        mma_ts_tf32(d, a_lo + kk, bh, idesc, true);
+      }
+      commit(cx.bar_mma);
+    }
+    cx.wait_mma();
+  }
+}
+
 // thread (p, 4 neurons): tanh jet of every stream of point p from plain Z rows in P, written as
 // operand rows of `out`, or, when `inplace`, back into P as FP32 rows (streams of a site from the
 // highest order down, the value stream last, so every Z a rule reads is still intact).
 template <bool BF16>
 __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ out,
-                             const DevGroup& G, int np, bool inplace) {
+                             const DevGroup& G, int np, bool inplace, bool also_out = false) {
   const int T = G.T;
   const int n4s = np >> 2;
   for (int e = threadIdx.x; e < T * n4s; e += NTC) {
@@ -169,9 +199,73 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
           }
         }
         if (inplace) st4(&P[(s * T + p) * LDS + n], h);
-        else put4<BF16>(out, s * T + p, n, np, h);
+        if (!inplace || also_out) put4<BF16>(out, s * T + p, n, np, h);
       }
     }
+  }
+}
+
+// Split TF32: the low part x - tf32(x) of every row of P (FP32 rows), into tensor memory
+// columns [0, kp) at a_lo. Each warp writes its own lane quarter, columns split over 4 warps.
+__device__ void alo_from_rows(const float* __restrict__ P, uint32_t a_lo, int kp, uint32_t lane_addr,
+                              int lrow, int cgrp) {
+  for (int c = 8 * cgrp; c < kp; c += 32) {
+    const float4 x0 = ld4(&P[lrow * LDS + c]), x1 = ld4(&P[lrow * LDS + c + 4]);
+    const float v[8] = {x0.x - to_tf32(x0.x), x0.y - to_tf32(x0.y), x0.z - to_tf32(x0.z),
+                        x0.w - to_tf32(x0.w), x1.x - to_tf32(x1.x), x1.y - to_tf32(x1.y),
+                        x1.z - to_tf32(x1.z), x1.w - to_tf32(x1.w)};
+    tmem_st8(a_lo + lane_addr + c, v);
+  }
+  tmem_st_wait();
+}
+
+// tanh jet of one (stream, point) row for 4 neurons from interleaved FP32 pre-activations
+__device__ __forceinline__ float4 h_row(const DevGroup& G, const unsigned char* __restrict__ zst, int kp,
+                                        const int8_t* row_s, const uint8_t* row_p, int r, int n) {
+  float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int sr = row_s[r];
+  if (sr < 0) return h;
+  const int T = G.T, p = row_p[r], q = G.st_site[sr];
+  Sig sg;
+  sg.make(ld4o(zst, ofs(G.site_streams[q][0] * T + p, n, kp, 4)), false);
+  if (G.st_order[sr] == 0) return sg.t;
+  for (int u = 0; u < G.st_nrule[sr]; ++u) {
+    const DevRule& ru = G.rules[sr][u];
+    float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
+    for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4o(zst, ofs(ru.sub[f] * T + p, n, kp, 4)));
+    h = f4add(h, v);
+  }
+  return h;
+}
+
+// 4 x 4 transpose inside each quad of lanes: lane (base + i) holds values for 4 neurons of row
+// (base + i); afterwards o[j] is neuron (i) of row (base + j). All 32 lanes must participate.
+__device__ __forceinline__ void quad_transpose(float4 h, int lane, float (&o)[4]) {
+  const int qd = lane & 3, qbase = lane & ~3;
+  o[0] = o[1] = o[2] = o[3] = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int si = (qd - k) & 3;
+    const float send = si == 0 ? h.x : si == 1 ? h.y : si == 2 ? h.z : h.w;
+    const float got = __shfl_sync(0xffffffffu, send, qbase | ((qd + k) & 3));
+    const int di = (qd + k) & 3;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (di == j) o[j] = got;
+  }
+}
+
+// dL/dH rows from the dX accumulator (tensor memory) into plain FP32 rows, zero past K and R
+__device__ __forceinline__ void d1_to_rows(uint32_t d1, float* __restrict__ P, int kp, int K, int R,
+                                           uint32_t lane_addr, int lrow, int cgrp) {
+  for (int c = 8 * cgrp; c < kp; c += 32) {
+    float v[8];
+    tmem_ld8(d1 + lane_addr + c, v);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (lrow >= R || c + i >= K) v[i] = 0.f;
+    st4(&P[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
+    st4(&P[lrow * LDS + c + 4], make_float4(v[4], v[5], v[6], v[7]));
   }
 }
 
@@ -195,7 +289,7 @@ struct TcArgs {
   int* err;                                   // set when a bounded wait gives up
 };
 
-template <bool BF16>
+template <bool BF16, bool X3>
 __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA) {
   constexpr int ES = BF16 ? 2 : 4;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -226,13 +320,14 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     mbar_init(&bars[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) tmem_alloc(tmem_slot, 256);
+  if (warp == 0) tmem_alloc(tmem_slot, X3 ? 512 : 256);
   for (int s = tid; s < A.n_slots; s += NTC) A.slot_partial[(int64_t)cta * A.n_slots + s] = 0.0;
   if (tid < MAX_OUT) cur_slot[tid] = 0.0;
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t D1 = *tmem_slot, D2 = *tmem_slot + 128;
+  const uint32_t ALO = *tmem_slot + 256;   // split TF32: low part of the A operand
   TcCtx cx{&bars[0], &bars[1], 0u, 0u, TA.err};
   // TMEM lane quarter and column group of this warp in the epilogues
   const int lrow = 32 * (warp & 3) + lane;
@@ -310,6 +405,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     __syncthreads();
     if (L == 2) {
       jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true);   // last hidden layer: FP32 rows in P1
+    } else if (X3) {
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true, true);
+      zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
+      __syncthreads();
+      alo_from_rows(P1, ALO, p16(A.width[1]), lane_addr, lrow, cgrp);
     } else {
       jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), false);
       zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
@@ -320,9 +420,13 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     for (int j = 1; j < L - 1; ++j) {
       const int K = A.width[j], N = A.width[j + 1];
       const int kp = p16(K), np = p16(N);
-      cx.load(opB, TA.wpack + TA.wfwd_off[j], (uint32_t)(np * kp * ES));
-      gemm_issue<BF16>(D1, opA, opB, np, kp, cx.bar_mma);
-      cx.wait_mma();
+      if (X3) {
+        gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wfwd_off[j], np, kp);
+      } else {
+        cx.load(opB, TA.wpack + TA.wfwd_off[j], (uint32_t)(np * kp * ES));
+        gemm_issue<BF16>(D1, opA, opB, np, kp, cx.bar_mma);
+        cx.wait_mma();
+      }
       // epilogue: D1 -> +bias -> P1 (plain) and scratch slot j (interleaved FP32)
       {
         const float* bj = prm + A.b_off[j];
@@ -349,6 +453,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       __syncthreads();
       if (j == L - 2) {
         jet_fwd_rows<BF16>(P1, opA, G, np, true);   // last hidden layer: FP32 rows in P1
+      } else if (X3) {
+        jet_fwd_rows<BF16>(P1, opA, G, np, true, true);
+        zero_rows<BF16>(opA, R, np, ES);
+        __syncthreads();
+        alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
       } else {
         jet_fwd_rows<BF16>(P1, opA, G, np, false);
         zero_rows<BF16>(opA, R, np, ES);
@@ -574,11 +683,19 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
       const int K = A.width[l - 1], kp = p16(K);
       zero_rows<BF16>(opA, R, np, ES);
+      if (X3) {
+        __syncthreads();
+        alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
+      }
       cx.publish();
       // dX: D1[rows x kp] = dL/dZ_l[rows x np] . (W_{l-1}^T packed [kp x np])^T
-      cx.load(opB, TA.wpack + TA.wbwd_off[l - 1], (uint32_t)(kp * np * ES));
-      gemm_issue<BF16>(D1, opA, opB, kp, np, cx.bar_mma);
-      cx.wait_mma();
+      if (X3) {
+        gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wbwd_off[l - 1], kp, np);
+      } else {
+        cx.load(opB, TA.wpack + TA.wbwd_off[l - 1], (uint32_t)(kp * np * ES));
+        gemm_issue<BF16>(D1, opA, opB, kp, np, cx.bar_mma);
+        cx.wait_mma();
+      }
       // dW operand A = dL/dZ_l^T [128 (neurons, zero padded) x 128 rows] from P1, and the bias
       // gradient of Linear l-1 (sum of dL/dZ_l over value rows) from the same reads
       {
@@ -594,7 +711,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             if (row_v[r + i]) sb += v[i];
           }
           put4<BF16>(opA, n, r, 128, make_float4(v[0], v[1], v[2], v[3]));
+          if (X3)   // lane = neuron n, columns = rows r..r+3 (the same r for the whole warp)
+            tmem_st4(ALO + lane_addr + r, v[0] - to_tf32(v[0]), v[1] - to_tf32(v[1]),
+                     v[2] - to_tf32(v[2]), v[3] - to_tf32(v[3]));
         }
+        if (X3) tmem_st_wait();
         red[(tid >> 7) * 128 + n] = sb;
         __syncthreads();
         float* db = grad + A.b_off[l - 1];
@@ -610,52 +731,52 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       // H_{l-1}^T [kp x 128 rows] -> opB. Lanes take consecutive rows (conflict-free reads of the
       // interleaved Z), 4 neurons each; each quad of lanes then transposes its 4 x 4 block with
       // shuffles so that a lane stores one neuron for 4 consecutive rows.
-      for (int e = tid; e < 32 * kp; e += NTC) {
-        const int r = e & 127, n = (e >> 7) * 4;
-        float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
-        const int sr = row_s[r];
-        if (sr >= 0) {
-          const int p = row_p[r];
-          const int q = G.st_site[sr];
-          Sig sg;
-          sg.make(ld4o(zst, ofs(G.site_streams[q][0] * T + p, n, kp, 4)), false);
-          if (G.st_order[sr] == 0) {
-            h = sg.t;
-          } else {
-            for (int u = 0; u < G.st_nrule[sr]; ++u) {
-              const DevRule& ru = G.rules[sr][u];
-              float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
-              for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4o(zst, ofs(ru.sub[f] * T + p, n, kp, 4)));
-              h = f4add(h, v);
-            }
+      if (X3) {
+        // split TF32: two halves of 64 rows, [hi | lo] of H_{l-1}^T for the half in opB, then
+        // hi*hi + hi*lo + lo*hi per K-step (A lo = dL/dZ_l^T low part in tensor memory)
+        const uint32_t lo_off = (uint32_t)kp * 64 * 4;
+        const uint32_t idesc = instr_desc<false>(128, kp);
+        for (int hh = 0; hh < 2; ++hh) {
+          for (int e = tid; e < 16 * kp; e += NTC) {
+            const int r = 64 * hh + (e & 63), n = (e >> 6) * 4;
+            float o[4];
+            quad_transpose(h_row(G, zst, kp, row_s, row_p, r, n), lane, o);
+            const int qd = lane & 3, rl = (r & ~3) - 64 * hh;
+            put4<false>(opB, n + qd, rl, 64, make_float4(o[0], o[1], o[2], o[3]));
+            put4<false>(opB + lo_off, n + qd, rl, 64,
+                        make_float4(o[0] - to_tf32(o[0]), o[1] - to_tf32(o[1]),
+                                    o[2] - to_tf32(o[2]), o[3] - to_tf32(o[3])));
           }
+          cx.publish();
+          if (tid == 0) {
+            const uint32_t a0 = smem_u32(opA), b0 = smem_u32(opB);
+            for (int j = 0; j < 8; ++j) {
+              const int kk = 64 * hh + 8 * j;
+              const uint64_t ad = smem_desc(a0 + (kk / 8) * 256, 128, 4096);
+              const uint64_t bh = smem_desc(b0 + j * 256, 128, 2048);
+              const uint64_t bl = smem_desc(b0 + lo_off + j * 256, 128, 2048);
+              mma<false>(D2, ad, bh, idesc, hh > 0 || j > 0);
+              mma<false>(D2, ad, bl, idesc, true);
+              mma_ts_tf32(D2, ALO + kk, bh, idesc, true);
+            }
+            commit(cx.bar_mma);
+          }
+          cx.wait_mma();
         }
-        const int qd = lane & 3, qbase = lane & ~3;
-        float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int si = (qd - k) & 3;
-          const float send = si == 0 ? h.x : si == 1 ? h.y : si == 2 ? h.z : h.w;
-          const float got = __shfl_sync(0xffffffffu, send, qbase | ((qd + k) & 3));
-          const int di = (qd + k) & 3;
-          if (di == 0) o0 = got; else if (di == 1) o1 = got; else if (di == 2) o2 = got; else o3 = got;
+        d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);
+      } else {
+        for (int e = tid; e < 32 * kp; e += NTC) {
+          const int r = e & 127, n = (e >> 7) * 4;
+          float o[4];
+          quad_transpose(h_row(G, zst, kp, row_s, row_p, r, n), lane, o);
+          put4<BF16>(opB, n + (lane & 3), r & ~3, 128, make_float4(o[0], o[1], o[2], o[3]));
         }
-        put4<BF16>(opB, n + qd, r & ~3, 128, make_float4(o0, o1, o2, o3));
+        cx.publish();
+        // dW: D2[128 x kp] = A[128 x 128] . B[kp x 128]^T
+        gemm_issue<BF16>(D2, opA, opB, kp, 128, cx.bar_mma);
+        d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);   // overlaps the dW MMA
+        cx.wait_mma();
       }
-      cx.publish();
-      // dW: D2[128 x kp] = A[128 x 128] . B[kp x 128]^T
-      gemm_issue<BF16>(D2, opA, opB, kp, 128, cx.bar_mma);
-      // dL/dH_{l-1} from D1 -> P1 (overlaps the dW MMA)
-      for (int c = 8 * cgrp; c < kp; c += 32) {
-        float v[8];
-        tmem_ld8(D1 + lane_addr + c, v);
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-          if (lrow >= R || c + i >= K) v[i] = 0.f;
-        st4(&P1[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
-        st4(&P1[lrow * LDS + c + 4], make_float4(v[4], v[5], v[6], v[7]));
-      }
-      cx.wait_mma();
       // flush dW_{l-1} (TMEM lane = output neuron, columns = input neurons) with vector atomic
       // adds into this CTA's zeroed gradient segment; one thread owns each address, so the
       // accumulation order is fixed
@@ -679,12 +800,13 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     A.slot_partial[(int64_t)cta * A.n_slots + Gs->slot_first + tid] += cur_slot[tid];
   fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(*tmem_slot, 256);
+  if (warp == 0) tmem_dealloc(*tmem_slot, X3 ? 512 : 256);
 }
 
-// ---- weight packing: every hidden Linear j into forward (N x K) and transposed (K x N) operands
+// ---- weight packing: every hidden Linear j into forward (N x K) and transposed (K x N) operands.
+// Split TF32 packs each operand as two K-halves, each a [hi | lo] pair of K-major blocks.
 namespace {
-template <bool BF16>
+template <bool BF16, bool X3>
 __global__ void pack_weights_kernel(const float* __restrict__ params, TcLaunch t) {
   constexpr int ES = BF16 ? 2 : 4;
   const int j = blockIdx.y + 1;   // hidden Linear layers 1..n_layers-2
@@ -696,9 +818,51 @@ __global__ void pack_weights_kernel(const float* __restrict__ params, TcLaunch t
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < np * kp; e += gridDim.x * blockDim.x) {
     const int n = e / kp, k = e % kp;
     const float v = (n < N && k < K) ? W[(int64_t)n * K + k] : 0.f;
-    put<BF16>(f, ofs(n, k, kp, ES), v);
-    put<BF16>(b, ofs(k, n, np, ES), v);
+    if (X3) {
+      const float hi = to_tf32(v), lo = to_tf32(v - hi);
+      const int kh = kp / 2, nh = np / 2;
+      // forward operand [np x kp], halves over k
+      {
+        const int h = k / kh, kk = k - h * kh;
+        unsigned char* base = f + (size_t)h * 2 * np * kh * 4;
+        *reinterpret_cast<float*>(base + ofs(n, kk, kh, 4)) = hi;
+        *reinterpret_cast<float*>(base + (size_t)np * kh * 4 + ofs(n, kk, kh, 4)) = lo;
+      }
+      // transposed operand [kp x np], halves over n
+      {
+        const int h = n / nh, nn = n - h * nh;
+        unsigned char* base = b + (size_t)h * 2 * kp * nh * 4;
+        *reinterpret_cast<float*>(base + ofs(k, nn, nh, 4)) = hi;
+        *reinterpret_cast<float*>(base + (size_t)kp * nh * 4 + ofs(k, nn, nh, 4)) = lo;
+      }
+    } else {
+      put<BF16>(f, ofs(n, k, kp, ES), v);
+      put<BF16>(b, ofs(k, n, np, ES), v);
+    }
   }
+}
+
+template <bool BF16, bool X3>
+cudaError_t launch_variant(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
+  static bool attr = false;
+  const size_t smem = fused_tc_smem_bytes();
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(fused_tc_kernel<BF16, X3>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (a.n_layers > 2) {   // pack this step's hidden weights
+    pack_weights_kernel<BF16, X3><<<dim3(16, a.n_layers - 2), 256, 0, s>>>(a.params, t);
+    count_launch();
+  }
+  TcArgs ta{};
+  ta.wpack = t.wpack;
+  for (int l = 0; l < TDG_MAX_LAYERS; ++l) { ta.wfwd_off[l] = t.fwd_off[l]; ta.wbwd_off[l] = t.bwd_off[l]; }
+  ta.err = t.err;
+  fused_tc_kernel<BF16, X3><<<n_ctas, NTC, smem, s>>>(a, ta);
+  count_launch();
+  return cudaGetLastError();
 }
 }  // namespace
 
@@ -708,30 +872,9 @@ size_t fused_tc_smem_bytes() {
 }
 
 cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
-  static bool attr[2] = {false, false};
-  const size_t smem = fused_tc_smem_bytes();
-  const bool bf16 = t.bf16;
-  if (!attr[bf16]) {
-    cudaError_t e = bf16 ? cudaFuncSetAttribute(fused_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                         : cudaFuncSetAttribute(fused_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr[bf16] = true;
-  }
-  // pack this step's hidden weights
-  if (a.n_layers > 2) {
-    dim3 grid(16, a.n_layers - 2);
-    if (bf16) pack_weights_kernel<true><<<grid, 256, 0, s>>>(a.params, t);
-    else pack_weights_kernel<false><<<grid, 256, 0, s>>>(a.params, t);
-    count_launch();
-  }
-  TcArgs ta{};
-  ta.wpack = t.wpack;
-  for (int l = 0; l < TDG_MAX_LAYERS; ++l) { ta.wfwd_off[l] = t.fwd_off[l]; ta.wbwd_off[l] = t.bwd_off[l]; }
-  ta.err = t.err;
-  if (bf16) fused_tc_kernel<true><<<n_ctas, NTC, smem, s>>>(a, ta);
-  else fused_tc_kernel<false><<<n_ctas, NTC, smem, s>>>(a, ta);
-  count_launch();
-  return cudaGetLastError();
+  if (t.x3) return launch_variant<false, true>(a, t, n_ctas, s);
+  if (t.bf16) return launch_variant<true, false>(a, t, n_ctas, s);
+  return launch_variant<false, false>(a, t, n_ctas, s);
 }
 
 }  // namespace tdg

@@ -108,6 +108,7 @@ cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s);
 // at fwd_off[j] and W_j^T as kp x np at bwd_off[j], widths padded to 16) and a timeout flag
 struct TcLaunch {
   bool bf16;
+  bool x3;     // split TF32 (hi*hi + hi*lo + lo*hi)
   unsigned char* wpack;
   int64_t fwd_off[TDG_MAX_LAYERS], bwd_off[TDG_MAX_LAYERS];
   int64_t w_off[TDG_MAX_LAYERS];

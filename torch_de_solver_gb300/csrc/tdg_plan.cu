@@ -336,7 +336,7 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     const int w = d.mlp.width[l];
     if (w < 4 || w > TDG_MAX_WIDTH || w % 4) return fail(TDG_ERR_UNSUPPORTED, "hidden width %d (multiple of 4, <= %d)", w, TDG_MAX_WIDTH);
   }
-  if (d.precision != TDG_PREC_FP32 && d.precision != TDG_PREC_TF32 && d.precision != TDG_PREC_BF16)
+  if (d.precision < TDG_PREC_FP32 || d.precision > TDG_PREC_BF16)
     return fail(TDG_ERR_UNSUPPORTED, "precision %d not built", d.precision);
   if (d.form != TDG_FORM_FUSED && d.form != TDG_FORM_PLAIN) return fail(TDG_ERR_UNSUPPORTED, "form %d not built", d.form);
   if (d.form == TDG_FORM_PLAIN && d.precision != TDG_PREC_FP32)
@@ -466,7 +466,8 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
   }
   if (d.precision != TDG_PREC_FP32) {
     // packed hidden weights for the tensor-core kernel: forward and transposed operand per layer
-    const int es = d.precision == TDG_PREC_BF16 ? 2 : 4;
+    // element bytes; split TF32 stores a hi and a lo value per element
+    const int es = d.precision == TDG_PREC_BF16 ? 2 : d.precision == TDG_PREC_3XTF32 ? 8 : 4;
     int64_t off = 0;
     for (int j = 1; j < L - 1; ++j) {
       const int64_t kp = (d.mlp.width[j] + 15) / 16 * 16, np = (d.mlp.width[j + 1] + 15) / 16 * 16;
@@ -565,6 +566,7 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
   } else {
     TcLaunch t{};
     t.bf16 = p->precision == TDG_PREC_BF16;
+    t.x3 = p->precision == TDG_PREC_3XTF32;
     t.wpack = p->d_wpack;
     for (int l = 0; l < TDG_MAX_LAYERS; ++l) {
       t.fwd_off[l] = p->wpack_fwd[l];
