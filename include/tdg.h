@@ -202,6 +202,12 @@ tdg_status tdg_loss_grad(tdg_plan* plan, const float* params, float* grad, doubl
  * wait on an mbarrier (the tensor-core path never spins without a limit). */
 tdg_status tdg_plan_sync_status(tdg_plan* plan);
 
+/* Failure-detection self-test: launch one thread that waits, with at most max_polls polls, on an
+ * mbarrier that nothing arrives at. Returns TDG_ERR_TIMEOUT when the wait gives up as designed
+ * (the kernels' waits on tensor-core and copy completion use the same bounded wait), leaving the
+ * CUDA context usable. Synchronises the device. */
+tdg_status tdg_selftest_bounded_wait(int32_t max_polls);
+
 /* In-place Adam (torch.optim.Adam semantics, L2 weight_decay) on n floats; step is a device
  * float counter incremented by the call, so the call can be replayed from a CUDA graph. */
 tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float* exp_avg_sq,

@@ -183,3 +183,71 @@ GOLDEN_CASES = {
     'sweep_ag': lambda api, dtype='float32': sweep_ag(api, dtype=dtype),
     'kovasznay_ag': lambda api, dtype='float32': kovasznay_ag(api, n=31, dtype=dtype),
 }
+
+
+# ---- boundary-condition and coefficient coverage (small grids)
+def neumann_ag(api, n=16, seed=3, dtype='float32'):
+    """u_t = 0.3 u_xx - x u; u(x,0) = sin(pi x); u_x(0,t) = cos t (operator BC); u(1,t) = 0."""
+    domain = api.Domain()
+    domain.variable('x', [0, 1], n, dtype=dtype)
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [0, 1], 't': 0}, value=lambda g: torch.sin(np.pi * g[:, 0]))
+    bnd.operator({'x': 0, 't': [0, 1]}, operator={'du/dx': {'coeff': 1, 'du/dx': [0], 'pow': 1}},
+                 value=lambda g: torch.cos(g[:, 1]))
+    bnd.dirichlet({'x': 1, 't': [0, 1]}, value=0)
+    eq = api.Equation()
+    eq.add({'du/dt': {'coeff': 1, 'du/dt': [1], 'pow': 1},
+            '-0.3 u_xx': {'coeff': -0.3, 'u_xx': [0, 0], 'pow': 1},
+            'x u': {'coeff': lambda g: g[:, 0], 'u': [None], 'pow': 1}})
+    net = mlp([2, 32, 32, 1], seed)
+    return domain, bnd, eq, net, dict(mode='autograd', lambda_operator=1, lambda_bound=10)
+
+
+def robin_data_ag(api, n=12, seed=4, dtype='float32'):
+    """u_t = u_xx + u^2 with a Robin condition at x=1, a data condition in the interior and a
+    per-point tensor coefficient."""
+    domain = api.Domain()
+    domain.variable('x', [0, 1], n, dtype=dtype)
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [0, 1], 't': 0}, value=lambda g: torch.sin(np.pi * g[:, 0]) ** 2)
+    bnd.dirichlet({'x': 0, 't': [0, 1]}, value=0)
+    bnd.robin({'x': 1, 't': [0, 1]}, value=lambda g: 0.5 * g[:, 1],
+              operator={'u': {'coeff': 2.0, 'u': [None], 'pow': 1},
+                        'du/dx': {'coeff': 0.5, 'du/dx': [0], 'pow': 1}})
+    pts = torch.tensor([[0.25, 0.5], [0.5, 0.5], [0.75, 0.25]], dtype=torch.float64)
+    bnd.data(pts, operator=None, value=torch.tensor([0.1, 0.2, 0.3]))
+    eq = api.Equation()
+    n_grid = (n + 1) ** 2
+    eq.add({'du/dt': {'coeff': 1, 'du/dt': [1], 'pow': 1},
+            '-u_xx': {'coeff': -1, 'u_xx': [0, 0], 'pow': 1},
+            '-c u^2': {'coeff': -torch.linspace(0.5, 1.5, n_grid), 'u': [None], 'pow': 2}})
+    net = mlp([2, 32, 32, 1], seed)
+    return domain, bnd, eq, net, dict(mode='autograd', lambda_operator=1, lambda_bound=[10, 5, 2])
+
+
+def neumann_nn(api, n=14, seed=5, dtype='float32'):
+    """'NN' mode with an operator (Neumann) condition: one-sided second-order stencils on the
+    typed boundary points, and periodic values in t."""
+    domain = api.Domain()
+    domain.variable('x', [0, 1], n, dtype=dtype)
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [0, 1], 't': 0}, value=lambda g: torch.sin(np.pi * g[:, 0]))
+    bnd.operator({'x': 0, 't': [0, 1]}, operator={'du/dx': {'coeff': 1, 'du/dx': [0], 'pow': 1}},
+                 value=0.0)
+    bnd.periodic([{'x': [0, 1], 't': 0}, {'x': [0, 1], 't': 1}])
+    eq = api.Equation()
+    eq.add({'du/dt': {'coeff': 1, 'du/dt': [1], 'pow': 1},
+            '-u_xx': {'coeff': lambda g: -0.2 - 0.1 * g[:, 0], 'u_xx': [0, 0], 'pow': 1}})
+    net = mlp([2, 24, 24, 1], seed)
+    return domain, bnd, eq, net, dict(mode='NN', lambda_operator=1, lambda_bound=10, h=1.0 / n)
+
+
+COVERAGE_CASES = {
+    'neumann_ag': lambda api, dtype='float32': neumann_ag(api, dtype=dtype),
+    'robin_data_ag': lambda api, dtype='float32': robin_data_ag(api, dtype=dtype),
+    'neumann_nn': lambda api, dtype='float32': neumann_nn(api, dtype=dtype),
+}
+GOLDEN_CASES.update(COVERAGE_CASES)

@@ -98,6 +98,7 @@ SIGNATURES = {
     'tdg_loss': (i32, [vp, vp, vp, vp, vp]),
     'tdg_loss_grad': (i32, [vp, vp, vp, vp, vp, vp]),
     'tdg_plan_sync_status': (i32, [vp]),
+    'tdg_selftest_bounded_wait': (i32, [i32]),
     'tdg_adam_step': (i32, [vp, vp, vp, vp, vp, i64, ctypes.POINTER(AdamDesc), vp]),
     'tdg_dot_f64': (i32, [vp, vp, i64, vp, vp]),
     'tdg_dot_f64_noalloc': (i32, [vp, vp, i64, vp, vp]),

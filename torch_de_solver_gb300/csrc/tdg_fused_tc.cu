@@ -871,6 +871,23 @@ size_t fused_tc_smem_bytes() {
          sizeof(DevGroup) + sizeof(double) * (MAX_OUT + (NTC / 32) * MAX_OUT) + 2 * sizeof(uint64_t) + 16 + 3 * 128;
 }
 
+// Self-test of the bounded wait: one thread waits on an mbarrier that nothing arrives at and
+// records whether the wait gave up (it must) instead of spinning forever.
+namespace {
+__global__ void bounded_wait_selftest_kernel(int max_polls, int* gave_up) {
+  __shared__ __align__(8) uint64_t bar;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  *gave_up = mbar_wait(&bar, 0, max_polls) ? 0 : 1;
+}
+}  // namespace
+
+cudaError_t launch_bounded_wait_selftest(int max_polls, int* gave_up, cudaStream_t s) {
+  bounded_wait_selftest_kernel<<<1, 1, 0, s>>>(max_polls, gave_up);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
   if (t.x3) return launch_variant<false, true>(a, t, n_ctas, s);
   if (t.bf16) return launch_variant<true, false>(a, t, n_ctas, s);

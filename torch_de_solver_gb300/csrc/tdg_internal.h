@@ -150,6 +150,7 @@ struct PlainArgs {
 };
 cudaError_t run_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
+cudaError_t launch_bounded_wait_selftest(int max_polls, int* gave_up, cudaStream_t s);
 cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
                                const int32_t* seg_list, int n_problems, int64_t n_params,
                                float* grad, cudaStream_t s);

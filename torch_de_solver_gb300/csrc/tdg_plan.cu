@@ -614,6 +614,20 @@ tdg_status tdg_plan_sync_status(tdg_plan* p) {
   return TDG_OK;
 }
 
+tdg_status tdg_selftest_bounded_wait(int32_t max_polls) {
+  if (max_polls < 1) return fail(TDG_ERR_INVALID, "max_polls < 1");
+  int* flag = nullptr;
+  cudaError_t e = cudaMalloc(&flag, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  int gave_up = -1;
+  e = launch_bounded_wait_selftest(max_polls, flag, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(&gave_up, flag, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(flag);
+  if (e != cudaSuccess) return cuda_fail(e, "bounded wait self-test");
+  if (gave_up == 1) return fail(TDG_ERR_TIMEOUT, "bounded wait gave up after %d polls", max_polls);
+  return fail(TDG_ERR_INVALID, "bounded wait self-test: the wait completed unexpectedly");
+}
+
 tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float* exp_avg_sq,
                          float* step, int64_t n, const tdg_adam_desc* hp, tdg_stream_t stream) {
   if (!params || !grad || !exp_avg || !exp_avg_sq || !step || !hp) return fail(TDG_ERR_INVALID, "null argument");

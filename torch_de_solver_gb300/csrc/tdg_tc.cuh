@@ -116,9 +116,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 
 // Wait for the phase with the given parity; gives up after a bounded number of polls and
 // returns false (the caller records the timeout) instead of spinning forever.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int max_polls = 1 << 24) {
   uint32_t done = 0;
-  for (int it = 0; it < (1 << 24) && !done; ++it) {
+  for (int it = 0; it < max_polls && !done; ++it) {
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
                  " selp.u32 %0, 1, 0, p;\n}"
                  : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
