@@ -175,6 +175,20 @@ class ClockSampler:
                 'reasons': sorted(reasons), 'samples': len(sm)}
 
 
+# ----------------------------------------------------------------------------- multi-rank
+def max_over_ranks(value, device):
+    """The largest value over all ranks (the step time every rank waits for); identity when the
+    job runs without torch.distributed. Ranks are independent replicas: this timing reduction is
+    the only collective."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ----------------------------------------------------------------------------- our arm
 def read_traffic(tag):
     """DRAM bytes per collocation point of the fused kernel from a committed ncu summary."""
@@ -221,6 +235,9 @@ def run_sweep(args, world):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     l0 = _lib.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
         for a, b in ev:
             flush.zero_()
@@ -229,7 +246,7 @@ def run_sweep(args, world):
             b.record(stream)
         torch.cuda.synchronize()
     launches = _lib.launch_count() - l0
-    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    ms = max_over_ranks(statistics.mean(a.elapsed_time(b) for a, b in ev), dev)
     # end to end: host copies of every solve's points each step, loss read back
     host = [t.cpu().pin_memory() for t in bm.plan.arrays]
     t0 = time.perf_counter()
@@ -313,11 +330,7 @@ def run_ours(args, rank, world):
     launches = _lib.launch_count() - launches0
     step_ms = [a.elapsed_time(c) for a, _, c in ev]
     kern_ms = [a.elapsed_time(b) for a, b, _ in ev]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t)
+    total_ms = max_over_ranks(sum(step_ms), dev)
     ms_per_step = total_ms / args.steps
     value = world * n_pts / (ms_per_step / 1e3)
 
