@@ -182,6 +182,9 @@ typedef struct CUstream_st* tdg_stream_t;   /* a cudaStream_t */
 int32_t tdg_abi_version(void);
 const char* tdg_last_error(void);
 int64_t tdg_launch_count(void);             /* kernels launched by this library so far */
+/* Compile-time jet class of a site with these streams (value first, then by order and axes, the
+ * order the lowering emits), or -1 when the site runs the table-driven jet code. Host only. */
+int32_t tdg_site_class(int32_t n_streams, const tdg_stream_desc* streams);
 
 /* Validate the description, build tile schedules and device tables, allocate the workspace. */
 tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** plan);

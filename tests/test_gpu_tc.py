@@ -43,3 +43,28 @@ def test_tensor_core_forward_only_equals_fused(precision):
         l0, _ = model.solution_cls.evaluate()
     l1, _ = model.solution_cls.evaluate()
     assert abs(l0.item() - l1.item()) <= 1e-6 * abs(l1.item())
+
+
+def _loss_grad(T, name, g, precision):
+    model = build_model(T, name, weights=g['weights'], precision=precision)
+    loss, _ = model.solution_cls.evaluate()
+    loss.backward()
+    grad = torch.cat([p.grad.reshape(-1) for p in model.net.parameters()]).cpu().numpy()
+    return loss.item(), grad
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', ['3xtf32', 'bf16'])
+@pytest.mark.parametrize('name', ['kovasznay_ag', 'kdv_ag', 'burgers_ag', 'neumann_ag'])
+def test_class_jets_equal_table_jets(name, precision, monkeypatch):
+    """The compile-time jet code of classed site layouts and the table-driven jet code compute
+    the same operations in the same order; the two agree to FP32 rounding (the compiler may
+    contract a product and a sum differently in the two codes)."""
+    import torch_de_solver_gb300 as T
+    g = golden(name)
+    l_cls, g_cls = _loss_grad(T, name, g, precision)
+    monkeypatch.setenv('TDG_JET_TABLES', '1')
+    l_tab, g_tab = _loss_grad(T, name, g, precision)
+    print(f'{name} {precision}: loss rel {rel(l_cls, l_tab):.3e} grad rel {rel(g_cls, g_tab):.3e} '
+          f'exact {l_cls == l_tab and np.array_equal(g_cls, g_tab)}')
+    assert rel(l_cls, l_tab) < 1e-6 and rel(g_cls, g_tab) < 1e-6

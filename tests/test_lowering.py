@@ -45,6 +45,44 @@ def test_lowering_shapes(name):
         assert total <= 16
 
 
+# the compile-time jet class the residual sites of each benchmark layout run (-1: tables)
+EXPECTED_CLASSES = {'kovasznay_ag': 7, 'burgers_ag': 5, 'kdv_ag': 8, 'heat_nn': 0}
+
+
+@pytest.mark.parametrize('name', list(EXPECTED_CLASSES))
+def test_site_classes(name):
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300 import _lib
+    from torch_de_solver_gb300.prepare import lower
+    builder = getattr(cases, name)
+    small = {'kovasznay_ag': dict(n=8), 'burgers_ag': dict(n=8), 'kdv_ag': dict(nx=8, nt=4),
+             'heat_nn': {}}[name]
+    d, bc, eq, net, kw = builder(T, **small)
+    kw = dict(kw)
+    mode = kw.pop('mode')
+    ir = lower(d.build(mode), eq.equation_lst, bc.build(d.variable_dict), mode,
+               kw['lambda_operator'], kw['lambda_bound'], kw.get('h', 0.001),
+               d_out=net[-1].out_features)
+    res = ir.groups[ir.residual_group]
+    for site in res.sites:
+        assert _lib.site_class(site.streams) == EXPECTED_CLASSES[name], site.streams
+    for grp in ir.groups:   # every layout classifies without error; boundary value sites are class 0
+        for site in grp.sites:
+            c = _lib.site_class(site.streams)
+            assert c >= -1
+            if [tuple(k) for k in site.streams] == [()]:
+                assert c == 0
+
+
+def test_site_class_rejects_unlisted_layouts():
+    from torch_de_solver_gb300 import _lib
+    assert _lib.site_class([(), (0,), (1,), (0, 1)]) == -1          # mixed derivative alone
+    assert _lib.site_class([(), (0,), (1,), (2,)]) == -1            # three axes
+    assert _lib.site_class([(), (1,), (0,)]) == -1                  # not in canonical order
+    assert _lib.site_class([(), (0,), (1,), (0, 0), (0, 1), (1, 1)]) == 10
+    assert _lib.site_class([(), (0,), (0, 0)]) == 4
+
+
 def test_unsupported_features_raise():
     import torch_de_solver_gb300 as T
     from torch_de_solver_gb300.prepare import lower

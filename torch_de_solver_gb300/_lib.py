@@ -91,6 +91,7 @@ SIGNATURES = {
     'tdg_abi_version': (i32, []),
     'tdg_last_error': (ctypes.c_char_p, []),
     'tdg_launch_count': (i64, []),
+    'tdg_site_class': (i32, [i32, ctypes.POINTER(StreamDesc)]),
     'tdg_plan_create': (i32, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(vp)]),
     'tdg_plan_destroy': (i32, [vp]),
     'tdg_plan_get_info': (i32, [vp, ctypes.POINTER(PlanInfo)]),
@@ -141,3 +142,13 @@ def check(status, what):
 
 def launch_count():
     return int(load().tdg_launch_count())
+
+
+def site_class(streams):
+    """Compile-time jet class of a site whose streams are sorted axis tuples, or -1 (tables)."""
+    arr = (StreamDesc * len(streams))()
+    for m, k in enumerate(streams):
+        arr[m].order = len(k)
+        for i, a in enumerate(k):
+            arr[m].axes[i] = a
+    return int(load().tdg_site_class(len(streams), arr))

@@ -12,8 +12,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
-SOURCES = ['tdg_plan.cu', 'tdg_fused.cu', 'tdg_fused_tc.cu', 'tdg_plain.cu', 'tdg_util.cu',
-           'tdg_noalloc.cu']
+SOURCES = ['tdg_tc_3x.cu', 'tdg_tc_tf32.cu', 'tdg_tc_bf16.cu', 'tdg_plan.cu', 'tdg_fused.cu',
+           'tdg_fused_tc.cu', 'tdg_plain.cu', 'tdg_util.cu', 'tdg_noalloc.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 LIB = os.path.join(PKG, 'libtdg.so')
 

@@ -1,0 +1,1069 @@
+// Tensor-core fused training-step kernel (sm_103a, tcgen05 + TMEM + bulk copies), as templates.
+// Each precision variant is instantiated in its own translation unit (tdg_tc_tf32.cu,
+// tdg_tc_bf16.cu, tdg_tc_3x.cu) so that the three compile in parallel.
+//
+// Same computation as fused_fp32_kernel (tdg_fused.cu): one persistent CTA per SM walks tiles of
+// 128 (stream, point) rows through the tanh-jet forward, the operator program and loss, and the
+// hand-written adjoint. Every hidden-layer GEMM runs on the tensor cores:
+//   forward  Z_{j+1}[rows x N]  = H_j[rows x K] . W_j^T          (A = H, B = W packed K-major)
+//   dX       G_H_{l-1}          = G_Z_l . W_{l-1}                 (A = G_Z, B = W^T packed K-major)
+//   dW       dW_{l-1}[N x K]    = G_Z_l^T . H_{l-1}               (A = G_Z^T, B = H^T, K = rows)
+// with FP32 accumulators in tensor memory (D1: 128 columns, D2: 128 columns). Operands are TF32
+// (kind::tf32, rounded with cvt.rna) or BF16 (kind::f16). One thread issues the MMAs and commits
+// them to an mbarrier; packed weights and the saved pre-activations are staged into shared memory
+// with cp.async.bulk. All mbarrier waits are bounded and report a timeout in a device flag.
+// The input layer (d_in <= 4), the output layer (d_out <= 8), the tanh jets and the operator
+// program stay on the CUDA cores.
+#pragma once
+#include <utility>
+#include "tdg_internal.h"
+#include "tdg_jetcls.h"
+#include "tdg_tc.cuh"
+
+namespace tdg {
+
+namespace {
+
+using namespace tc;
+
+constexpr int OPB = 128 * 128 * 4;    // bytes of one operand buffer
+constexpr int NTC = 512;              // threads of the tensor-core kernel (16 warps)
+
+__device__ __forceinline__ int p16(int w) { return (w + 15) & ~15; }
+
+__device__ __forceinline__ float powf_(float x, float p) {
+  if (p == 1.f) return x;
+  if (p == 2.f) return x * x;
+  if (p == 0.f) return 1.f;
+  if (p == 3.f) return x * x * x;
+  return powf(x, p);
+}
+
+__device__ __forceinline__ float dpowf_(float x, float p) {
+  if (p == 1.f) return 1.f;
+  if (p == 2.f) return 2.f * x;
+  if (p == 0.f) return 0.f;
+  if (p == 3.f) return 3.f * x * x;
+  return p * powf(x, p - 1.f);
+}
+
+__device__ __forceinline__ float4 f4mul(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 f4scale(float4 a, float c) { return make_float4(a.x * c, a.y * c, a.z * c, a.w * c); }
+
+struct Sig {   // tanh and its derivatives, as functions of t = tanh(z), for 4 neurons
+  float4 t, s1, s2, s3, s4;
+  __device__ __forceinline__ void make(const float4 z, bool need4) {
+    t = make_float4(tanhf(z.x), tanhf(z.y), tanhf(z.z), tanhf(z.w));
+    const float4 tt = f4mul(t, t);
+    s1 = make_float4(1.f - tt.x, 1.f - tt.y, 1.f - tt.z, 1.f - tt.w);
+    s2 = f4scale(f4mul(t, s1), -2.f);
+    s3 = f4mul(s1, make_float4(6.f * tt.x - 2.f, 6.f * tt.y - 2.f, 6.f * tt.z - 2.f, 6.f * tt.w - 2.f));
+    s4 = need4 ? f4mul(f4mul(t, s1), make_float4(16.f - 24.f * tt.x, 16.f - 24.f * tt.y,
+                                                  16.f - 24.f * tt.z, 16.f - 24.f * tt.w))
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  // the k-th derivative; k is the same for every thread of a group's table entry (uniform branch)
+  __device__ __forceinline__ float4 sel(int k) const {
+    switch (k) {
+      case 0: return t;
+      case 1: return s1;
+      case 2: return s2;
+      case 3: return s3;
+      default: return s4;
+    }
+  }
+};
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float4 ld4o(const unsigned char* b, uint32_t off) {
+  return *reinterpret_cast<const float4*>(b + off);
+}
+
+// write 4 consecutive K elements of row i (kp elements per row) into an operand buffer
+template <bool BF16>
+__device__ __forceinline__ void put4(unsigned char* buf, int i, int k, int kp, float4 v) {
+  if (BF16) {
+    const uint32_t off = ofs(i, k, kp, 2);
+    __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+    uint2 u;
+    u.x = *reinterpret_cast<uint32_t*>(&a);
+    u.y = *reinterpret_cast<uint32_t*>(&b);
+    *reinterpret_cast<uint2*>(buf + off) = u;
+  } else {
+    const uint32_t off = ofs(i, k, kp, 4);
+    *reinterpret_cast<float4*>(buf + off) =
+        make_float4(to_tf32(v.x), to_tf32(v.y), to_tf32(v.z), to_tf32(v.w));
+  }
+}
+
+struct TcCtx {
+  uint64_t* bar_mma;
+  uint64_t* bar_tma;
+  uint32_t ph_mma, ph_tma;
+  int* err;
+  __device__ __forceinline__ void wait_mma() {
+    if (!mbar_wait(bar_mma, ph_mma) && threadIdx.x == 0) atomicExch(err, 1);
+    ph_mma ^= 1;
+    fence_after();
+  }
+  bool inflight;   // a bulk copy issued and not yet waited for
+  __device__ __forceinline__ void wait_tma() {
+    if (!mbar_wait(bar_tma, ph_tma) && threadIdx.x == 0) atomicExch(err, 2);
+    ph_tma ^= 1;
+    inflight = false;
+  }
+  // every thread: generic-proxy smem writes visible to the tensor cores, then barrier
+  __device__ __forceinline__ void publish() {
+    fence_async_all();
+    fence_before();
+    __syncthreads();
+    fence_after();
+  }
+  // start a bulk copy into shared memory; at most one is in flight
+  __device__ __forceinline__ void issue(void* dst, const void* src, uint32_t bytes) {
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(bar_tma, bytes);
+      bulk_g2s(dst, src, bytes, bar_tma);
+    }
+    inflight = true;
+  }
+  __device__ __forceinline__ void load(void* dst, const void* src, uint32_t bytes) {
+    issue(dst, src, bytes);
+    wait_tma();
+  }
+  // the copy issued ahead of time for this use (issued here when none is in flight), completed
+  __device__ __forceinline__ void ensure(void* dst, const void* src, uint32_t bytes) {
+    if (!inflight) issue(dst, src, bytes);
+    wait_tma();
+  }
+};
+
+// D[128 x n] = A[128 x k] . B[n x k]^T, issued by thread 0 and committed to bar_mma
+template <bool BF16>
+__device__ __forceinline__ void gemm_issue(uint32_t d, const unsigned char* a, const unsigned char* b,
+                                           int n, int k, uint64_t* bar) {
+  if (threadIdx.x != 0) return;
+  constexpr int es = BF16 ? 2 : 4, epc = 16 / es, mk = BF16 ? 16 : 8;
+  const uint32_t sbo = (uint32_t)(k / epc) * 128;
+  const uint32_t idesc = instr_desc<BF16>(128, n);
+  const uint32_t a0 = smem_u32(a), b0 = smem_u32(b);
+  for (int j = 0; j < k / mk; ++j)
+    mma<BF16>(d, smem_desc(a0 + j * 256, 128, sbo), smem_desc(b0 + j * 256, 128, sbo), idesc, j > 0);
+  commit(bar);
+}
+
+// Split TF32: D = A . B^T as hi*hi + hi*lo + lo*hi, FP32 accumulate. A hi in shared memory (k
+// elements per row, rounded), A lo in tensor memory (columns), B streamed from global memory in
+// two K-halves of [hi | lo] blocks through opB. All threads call this (it waits on the copies and
+// the MMAs); thread 0 issues.
+__device__ void gemm3x(TcCtx& cx, uint32_t d, const unsigned char* a, uint32_t a_lo, unsigned char* opB,
+                       const unsigned char* b_src, int n, int k) {
+  const uint32_t idesc = instr_desc<false>(128, n);
+  const int kh = k / 2;
+  const uint32_t half_bytes = (uint32_t)n * kh * 4;
+  const uint32_t sbo_a = (uint32_t)(k / 4) * 128, sbo_b = (uint32_t)(kh / 4) * 128;
+  for (int h = 0; h < 2; ++h) {
+    if (h == 0) cx.ensure(opB, b_src, 2 * half_bytes);
+    else cx.load(opB, b_src + 2 * half_bytes, 2 * half_bytes);
+    if (threadIdx.x == 0) {
+      fence_after();
+      const uint32_t a0 = smem_u32(a), b0 = smem_u32(opB);
+      for (int j = 0; j < kh / 8; ++j) {
+        const int kk = h * kh + 8 * j;
+        const uint64_t ad = smem_desc(a0 + (kk / 8) * 256, 128, sbo_a);
+        const uint64_t bh = smem_desc(b0 + j * 256, 128, sbo_b);
+        const uint64_t bl = smem_desc(b0 + half_bytes + j * 256, 128, sbo_b);
+        mma<false>(d, ad, bh, idesc, h > 0 || j > 0);
+        mma<false>(d, ad, bl, idesc, true);
+        mma_ts_tf32(d, a_lo + kk, bh, idesc, true);
+      }
+      commit(cx.bar_mma);
+    }
+    cx.wait_mma();
+  }
+}
+
+// ---- jet code of the compile-time site classes (tdg_jetcls.h): rules folded into straight-line
+// code, every stream value of a (point, 4 neurons) task in registers
+template <int C>
+__host__ __device__ constexpr jetcls::Rules rules_of() { return jetcls::make_rules(jetcls::kSiteClasses[C]); }
+
+// whether a rule of stream M reads the pre-activation of stream Q (Q may be M itself)
+template <int C>
+__host__ __device__ constexpr bool reads_sub(int M, int Q) {
+  bool r = false;
+  for (int u = 0; u < rules_of<C>().nrule[M]; ++u)
+    for (int i = 0; i < rules_of<C>().k[M][u]; ++i) r = r || rules_of<C>().sub[M][u][i] == Q;
+  return r;
+}
+
+template <typename F, int... I>
+__device__ __forceinline__ void sfor_(F& f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void sfor(F&& f) { sfor_(f, std::make_integer_sequence<int, N>{}); }
+
+// run f(integral_constant<C>) for the site class `cls`; false when cls is not a compiled class
+template <typename F>
+__device__ __forceinline__ bool with_class(int cls, F&& f) {
+  bool done = false;
+  sfor<jetcls::N_CLASSES>([&](auto cc) {
+    if (cls == decltype(cc)::value) { f(cc); done = true; }
+  });
+  return done;
+}
+
+// H_M = sum_u mult * tanh^(k)(z_0) * prod Z[sub]  (same operation order as the table rules)
+template <int C, int M, int NS>
+__device__ __forceinline__ float4 cls_rule_sum(const Sig& sg, const float4 (&z)[NS]) {
+  float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+  sfor<rules_of<C>().nrule[M]>([&](auto uc) {
+    constexpr int U = decltype(uc)::value;
+    constexpr int K = rules_of<C>().k[M][U];
+    float4 v = f4scale(sg.sel(K), (float)rules_of<C>().mult[M][U]);
+    sfor<K>([&](auto fc) { v = f4mul(v, z[rules_of<C>().sub[M][U][decltype(fc)::value]]); });
+    h = f4add(h, v);
+  });
+  return h;
+}
+
+// forward jet of one site for (point p, neurons n..n+3): plain Z rows of P -> H rows (in place
+// and/or operand rows of `out`)
+template <int C, bool BF16>
+__device__ __forceinline__ void jet_fwd_cls(float* __restrict__ P, unsigned char* __restrict__ out, int T,
+                                            int base, int p, int n, int np, bool inplace, bool write_out) {
+  constexpr int NS = rules_of<C>().ns;
+  float4 z[NS];
+  sfor<NS>([&](auto mc) {
+    constexpr int M = decltype(mc)::value;
+    z[M] = ld4(&P[((base + M) * T + p) * LDS + n]);
+  });
+  Sig sg;
+  sg.make(z[0], rules_of<C>().maxk >= 4);
+  sfor<NS>([&](auto mc) {
+    constexpr int M = decltype(mc)::value;
+    float4 h;
+    if constexpr (M == 0) h = sg.t;
+    else h = cls_rule_sum<C, M>(sg, z);
+    if (inplace) st4(&P[((base + M) * T + p) * LDS + n], h);
+    if (write_out) put4<BF16>(out, (base + M) * T + p, n, np, h);
+  });
+}
+
+// jet adjoint of one site for (point p, neurons n..n+3): dL/dH rows of P1 and the interleaved
+// pre-activations zs -> dL/dZ rows in place (and operand rows of opA). Contributions accumulate
+// in the order of the table pulls: the value stream's own term, then streams and rules ascending.
+template <int C, bool BF16>
+__device__ __forceinline__ void jet_bwd_cls(float* __restrict__ P1, const unsigned char* __restrict__ zs,
+                                            unsigned char* __restrict__ opA, int T, int base, int p, int n,
+                                            int np, bool write_op) {
+  constexpr int NS = rules_of<C>().ns;
+  float4 z[NS], g[NS], gz[NS];
+  sfor<NS>([&](auto mc) {
+    constexpr int M = decltype(mc)::value;
+    z[M] = ld4o(zs, ofs((base + M) * T + p, n, np, 4));
+    g[M] = ld4(&P1[((base + M) * T + p) * LDS + n]);
+    gz[M] = make_float4(0.f, 0.f, 0.f, 0.f);
+  });
+  Sig sg;
+  sg.make(z[0], rules_of<C>().maxk + 1 >= 4);
+  gz[0] = f4mul(g[0], sg.s1);
+  sfor<NS>([&](auto mc) {
+    constexpr int M = decltype(mc)::value;
+    if constexpr (M >= 1) {
+      sfor<rules_of<C>().nrule[M]>([&](auto uc) {
+        constexpr int U = decltype(uc)::value;
+        constexpr int K = rules_of<C>().k[M][U];
+        constexpr float MU = (float)rules_of<C>().mult[M][U];
+        float4 v = f4mul(g[M], f4scale(sg.sel(K + 1), MU));
+        sfor<K>([&](auto fc) { v = f4mul(v, z[rules_of<C>().sub[M][U][decltype(fc)::value]]); });
+        gz[0] = f4add(gz[0], v);
+        sfor<K>([&](auto ic) {
+          constexpr int I = decltype(ic)::value;
+          float4 w = f4mul(g[M], f4scale(sg.sel(K), MU));
+          sfor<K>([&](auto jc) {
+            constexpr int J = decltype(jc)::value;
+            if constexpr (J != I) w = f4mul(w, z[rules_of<C>().sub[M][U][J]]);
+          });
+          constexpr int SI = rules_of<C>().sub[M][U][I];
+          gz[SI] = f4add(gz[SI], w);
+        });
+      });
+    }
+  });
+  sfor<NS>([&](auto mc) {
+    constexpr int M = decltype(mc)::value;
+    st4(&P1[((base + M) * T + p) * LDS + n], gz[M]);
+    if (write_op) put4<BF16>(opA, (base + M) * T + p, n, np, gz[M]);
+  });
+}
+
+// forward jet of stream m of one site for one (stream, point) row, from interleaved FP32 Z rows
+template <int C>
+__device__ __forceinline__ float4 h_row_cls(const unsigned char* __restrict__ zst, int kp, int T, int base,
+                                            int m, int p, int n) {
+  constexpr int NS = rules_of<C>().ns;
+  Sig sg;
+  sg.make(ld4o(zst, ofs(base * T + p, n, kp, 4)), false);
+  float4 h = sg.t;
+  sfor<NS>([&](auto mc) {
+    constexpr int M = decltype(mc)::value;
+    if constexpr (M >= 1) {
+      if (m == M) {
+        float4 z[NS];
+        sfor<NS>([&](auto sc) {
+          constexpr int Q = decltype(sc)::value;
+          if constexpr (reads_sub<C>(M, Q)) z[Q] = ld4o(zst, ofs((base + Q) * T + p, n, kp, 4));
+          else z[Q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        });
+        h = cls_rule_sum<C, M>(sg, z);
+      }
+    }
+  });
+  return h;
+}
+
+// thread (p, 4 neurons): tanh jet of every stream of point p from plain Z rows in P, written as
+// operand rows of `out`, or, when `inplace`, back into P as FP32 rows (streams of a site from the
+// highest order down, the value stream last, so every Z a rule reads is still intact).
+template <bool BF16>
+__device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ out,
+                             const DevGroup& G, int np, bool inplace, bool also_out = false) {
+  const int T = G.T;
+  const int n4s = np >> 2;
+  for (int q = 0; q < G.n_sites; ++q) {
+    const int ns = G.site_nstreams[q];
+    const int base = G.site_streams[q][0];
+    // classed site: one loop per class, the dispatch outside it
+    if (with_class(G.site_cls[q], [&](auto cc) {
+          for (int e = threadIdx.x; e < T * n4s; e += NTC)
+            jet_fwd_cls<decltype(cc)::value, BF16>(P, out, T, base, e % T, (e / T) * 4, np, inplace,
+                                                   !inplace || also_out);
+        }))
+      continue;
+    for (int e = threadIdx.x; e < T * n4s; e += NTC) {
+      const int p = e % T, n = (e / T) * 4;
+      Sig sg;
+      sg.make(ld4(&P[(base * T + p) * LDS + n]), false);
+      for (int m = ns - 1; m >= 0; --m) {
+        const int s = G.site_streams[q][m];
+        float4 h = sg.t;
+        if (m > 0) {
+          h = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int u = 0; u < G.st_nrule[s]; ++u) {
+            const DevRule& ru = G.rules[s][u];
+            float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
+            for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4(&P[(ru.sub[f] * T + p) * LDS + n]));
+            h = f4add(h, v);
+          }
+        }
+        if (inplace) st4(&P[(s * T + p) * LDS + n], h);
+        if (!inplace || also_out) put4<BF16>(out, s * T + p, n, np, h);
+      }
+    }
+  }
+}
+
+// Split TF32: the low part x - tf32(x) of every row of P (FP32 rows), into tensor memory
+// columns [0, kp) at a_lo. Each warp writes its own lane quarter, columns split over 4 warps.
+__device__ void alo_from_rows(const float* __restrict__ P, uint32_t a_lo, int kp, uint32_t lane_addr,
+                              int lrow, int cgrp) {
+  for (int c = 8 * cgrp; c < kp; c += 32) {
+    const float4 x0 = ld4(&P[lrow * LDS + c]), x1 = ld4(&P[lrow * LDS + c + 4]);
+    const float v[8] = {x0.x - to_tf32(x0.x), x0.y - to_tf32(x0.y), x0.z - to_tf32(x0.z),
+                        x0.w - to_tf32(x0.w), x1.x - to_tf32(x1.x), x1.y - to_tf32(x1.y),
+                        x1.z - to_tf32(x1.z), x1.w - to_tf32(x1.w)};
+    tmem_st8(a_lo + lane_addr + c, v);
+  }
+  tmem_st_wait();
+}
+
+// tanh jet of one (stream, point) row for 4 neurons from interleaved FP32 pre-activations
+__device__ __forceinline__ float4 h_row(const DevGroup& G, const unsigned char* __restrict__ zst, int kp,
+                                        const int8_t* row_s, const uint8_t* row_p, int r, int n) {
+  float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int sr = row_s[r];
+  if (sr < 0) return h;
+  const int T = G.T, p = row_p[r], q = G.st_site[sr];
+  Sig sg;
+  sg.make(ld4o(zst, ofs(G.site_streams[q][0] * T + p, n, kp, 4)), false);
+  if (G.st_order[sr] == 0) return sg.t;
+  for (int u = 0; u < G.st_nrule[sr]; ++u) {
+    const DevRule& ru = G.rules[sr][u];
+    float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
+    for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4o(zst, ofs(ru.sub[f] * T + p, n, kp, 4)));
+    h = f4add(h, v);
+  }
+  return h;
+}
+
+// h_row for a group whose sites all have compile-time class C
+template <int C>
+__device__ __forceinline__ float4 h_row_c(const DevGroup& G, const unsigned char* __restrict__ zst, int kp,
+                                          const int8_t* row_s, const uint8_t* row_p, int r, int n) {
+  const int sr = row_s[r];
+  if (sr < 0) return make_float4(0.f, 0.f, 0.f, 0.f);
+  const int base = G.site_streams[G.st_site[sr]][0];
+  return h_row_cls<C>(zst, kp, G.T, base, sr - base, row_p[r], n);
+}
+
+// 4 x 4 transpose inside each quad of lanes: lane (base + i) holds values for 4 neurons of row
+// (base + i); afterwards o[j] is neuron (i) of row (base + j). All 32 lanes must participate.
+__device__ __forceinline__ void quad_transpose(float4 h, int lane, float (&o)[4]) {
+  const int qd = lane & 3, qbase = lane & ~3;
+  o[0] = o[1] = o[2] = o[3] = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int si = (qd - k) & 3;
+    const float send = si == 0 ? h.x : si == 1 ? h.y : si == 2 ? h.z : h.w;
+    const float got = __shfl_sync(0xffffffffu, send, qbase | ((qd + k) & 3));
+    const int di = (qd + k) & 3;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (di == j) o[j] = got;
+  }
+}
+
+// dL/dH rows from the dX accumulator (tensor memory) into plain FP32 rows, zero past K and R
+__device__ __forceinline__ void d1_to_rows(uint32_t d1, float* __restrict__ P, int kp, int K, int R,
+                                           uint32_t lane_addr, int lrow, int cgrp) {
+  for (int c = 8 * cgrp; c < kp; c += 32) {
+    float v[8];
+    tmem_ld8(d1 + lane_addr + c, v);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (lrow >= R || c + i >= K) v[i] = 0.f;
+    st4(&P[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
+    st4(&P[lrow * LDS + c + 4], make_float4(v[4], v[5], v[6], v[7]));
+  }
+}
+
+// zero rows [r0, 128) of an operand with kp elements per row
+template <bool BF16>
+__device__ void zero_rows(unsigned char* buf, int r0, int kp, int es) {
+  const int n4s = kp >> 2;
+  for (int e = threadIdx.x; e < (128 - r0) * n4s; e += NTC) {
+    const int r = r0 + e / n4s, n = (e % n4s) * 4;
+    if (es == 4) *reinterpret_cast<float4*>(buf + ofs(r, n, kp, 4)) = make_float4(0, 0, 0, 0);
+    else *reinterpret_cast<uint2*>(buf + ofs(r, n, kp, 2)) = make_uint2(0, 0);
+  }
+}
+
+}  // namespace
+
+struct TcArgs {
+  const unsigned char* wpack;                 // packed hidden weights
+  int64_t wfwd_off[TDG_MAX_LAYERS];           // byte offsets of W_j (forward) per Linear j
+  int64_t wbwd_off[TDG_MAX_LAYERS];           // byte offsets of W_j^T
+  int* err;                                   // set when a bounded wait gives up
+};
+
+template <bool BF16, bool X3>
+__global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA) {
+  constexpr int ES = BF16 ? 2 : 4;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* opA = smem_raw;
+  unsigned char* opB = smem_raw + OPB;
+  float* P1 = reinterpret_cast<float*>(smem_raw + 2 * OPB);
+  float* ybuf = P1 + RMAX * LDS;
+  float* gybuf = ybuf + RMAX * MAX_OUT;
+  float* xsbuf = gybuf + RMAX * MAX_OUT;
+  DevGroup* Gs = reinterpret_cast<DevGroup*>(xsbuf + RMAX * TDG_MAX_DIN);
+  double* cur_slot = reinterpret_cast<double*>(Gs + 1);        // [MAX_OUT]
+  double* wred = cur_slot + MAX_OUT;                           // [NTC/32][MAX_OUT]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(wred + (NTC / 32) * MAX_OUT);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+  int8_t* row_s = reinterpret_cast<int8_t*>(tmem_slot + 4);     // [128] stream of a row, -1 padding
+  uint8_t* row_p = reinterpret_cast<uint8_t*>(row_s + 128);     // [128] point of a row
+  uint8_t* row_v = row_p + 128;                                  // [128] 1 on value-stream rows
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int cta = blockIdx.x;
+  const int L = A.n_layers;
+  const int d_in = A.width[0], d_out = A.width[L];
+  const int64_t scr_slot = 128 * 128;                         // floats per saved layer
+  float* scr = A.scratch + (int64_t)cta * (L - 1) * scr_slot;
+
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, X3 ? 512 : 256);
+  for (int s = tid; s < A.n_slots; s += NTC) A.slot_partial[(int64_t)cta * A.n_slots + s] = 0.0;
+  if (tid < MAX_OUT) cur_slot[tid] = 0.0;
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t D1 = *tmem_slot, D2 = *tmem_slot + 128;
+  const uint32_t ALO = *tmem_slot + 256;   // split TF32: low part of the A operand
+  TcCtx cx{&bars[0], &bars[1], 0u, 0u, TA.err, false};
+  // TMEM lane quarter and column group of this warp in the epilogues
+  const int lrow = 32 * (warp & 3) + lane;
+  const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
+  const int cgrp = warp >> 2;                    // 0..3: this warp's 8-column chunks c = 8*cgrp + 32*i
+  int cur_group = -1;
+  // the first bulk copy of hidden GEMM j's forward weights (split TF32: the first [hi | lo] half)
+  auto wfwd_first = [&](int j) {
+    const uint32_t nk = (uint32_t)p16(A.width[j + 1]) * p16(A.width[j]);
+    cx.issue(opB, TA.wpack + TA.wfwd_off[j], X3 ? nk * 4 : nk * ES);
+  };
+
+  for (int ti = A.cta_tile_begin[cta]; ti < A.cta_tile_begin[cta + 1]; ++ti) {
+    const DevTile tile = A.tiles[ti];
+    cx.publish();                    // opB's last generic accesses ordered before the copy below
+    if (L > 2) wfwd_first(1);        // overlaps the coordinates, input layer and first jets
+    if (tile.group != cur_group) {
+      if (cur_group >= 0 && tid < Gs->n_outputs) {
+        A.slot_partial[(int64_t)cta * A.n_slots + Gs->slot_first + tid] += cur_slot[tid];
+        cur_slot[tid] = 0.0;
+      }
+      __syncthreads();
+      const int4* src = reinterpret_cast<const int4*>(&A.groups[tile.group]);
+      int4* dst = reinterpret_cast<int4*>(Gs);
+      for (int e = tid; e < (int)(sizeof(DevGroup) / 16); e += NTC) dst[e] = src[e];
+      cur_group = tile.group;
+      __syncthreads();
+      if (tid < 128) {
+        const int T0 = Gs->T, R0 = Gs->T * Gs->S;
+        const int sr = tid < R0 ? tid / T0 : -1;
+        row_s[tid] = (int8_t)sr;
+        row_p[tid] = (uint8_t)(tid < R0 ? tid - sr * T0 : 0);
+        row_v[tid] = (uint8_t)(sr >= 0 && Gs->st_order[sr] == 0);
+      }
+      __syncthreads();
+    }
+    const DevGroup& G = *Gs;
+    const int T = G.T, S = G.S, R = T * S;
+    const int nvalid = tile.nvalid, row0 = tile.row0;
+    const float* prm = A.params + (int64_t)G.problem * A.n_params;
+
+    for (int e = tid; e < RMAX * d_in; e += NTC) {
+      const int r = e / d_in, a = e - r * d_in;
+      float x = 0.f;
+      if (r < R) {
+        const int s = r / T, p = r - s * T, q = G.st_site[s];
+        if (p < nvalid) x = A.arrays[G.site_points[q]][(int64_t)(row0 + p) * d_in + a] + G.site_off[q][a];
+      }
+      xsbuf[r * TDG_MAX_DIN + a] = x;
+    }
+    __syncthreads();
+
+    // ---- input layer -> Z_1 (plain in P1, interleaved FP32 in scratch slot 0)
+    {
+      const int N = A.width[1], np = p16(N);
+      const float* W0 = prm + A.w_off[0];
+      const float* b0 = prm + A.b_off[0];
+      for (int e = tid; e < RMAX * (np >> 2); e += NTC) {
+        const int r = e % RMAX, n = (e / RMAX) * 4;
+        float z[4] = {0.f, 0.f, 0.f, 0.f};
+        if (r < R) {
+          const int s = r / T, o = G.st_order[s];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int nn = n + i;
+            if (nn >= N) continue;
+            if (o == 0) {
+              float v = 0.f;
+              for (int a = 0; a < d_in; ++a) v = fmaf(__ldg(&W0[nn * d_in + a]), xsbuf[r * TDG_MAX_DIN + a], v);
+              z[i] = v + __ldg(&b0[nn]);
+            } else if (o == 1) {
+              z[i] = __ldg(&W0[nn * d_in + G.st_axis[s]]);
+            }
+          }
+        }
+        const float4 zv = make_float4(z[0], z[1], z[2], z[3]);
+        st4(&P1[r * LDS + n], zv);
+        if (A.do_grad) *reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(scr) + ofs(r, n, np, 4)) = zv;
+      }
+    }
+    __syncthreads();
+    if (L == 2) {
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true);   // last hidden layer: FP32 rows in P1
+    } else if (X3) {
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true, true);
+      zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
+      __syncthreads();
+      alo_from_rows(P1, ALO, p16(A.width[1]), lane_addr, lrow, cgrp);
+    } else {
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), false);
+      zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
+    }
+    cx.publish();
+
+    // ---- hidden layers on the tensor cores
+    for (int j = 1; j < L - 1; ++j) {
+      const int K = A.width[j], N = A.width[j + 1];
+      const int kp = p16(K), np = p16(N);
+      if (X3) {
+        gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wfwd_off[j], np, kp);
+      } else {
+        cx.ensure(opB, TA.wpack + TA.wfwd_off[j], (uint32_t)(np * kp * ES));
+        gemm_issue<BF16>(D1, opA, opB, np, kp, cx.bar_mma);
+        cx.wait_mma();
+      }
+      if (j + 1 < L - 1) wfwd_first(j + 1);   // opB is free: overlaps the epilogue and the jets
+      // epilogue: D1 -> +bias -> P1 (plain) and scratch slot j (interleaved FP32)
+      {
+        const float* bj = prm + A.b_off[j];
+        const bool val = row_v[lrow] != 0;
+        unsigned char* sj = reinterpret_cast<unsigned char*>(scr + (int64_t)j * scr_slot);
+        for (int c = 8 * cgrp; c < np; c += 32) {
+          float v[8];
+          tmem_ld8(D1 + lane_addr + c, v);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int n = c + i;
+            v[i] = n < N ? v[i] + (val ? __ldg(&bj[n]) : 0.f) : 0.f;
+            if (lrow >= R) v[i] = 0.f;
+          }
+          st4(&P1[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
+          st4(&P1[lrow * LDS + c + 4], make_float4(v[4], v[5], v[6], v[7]));
+          if (A.do_grad) {
+            *reinterpret_cast<float4*>(sj + ofs(lrow, c, np, 4)) = make_float4(v[0], v[1], v[2], v[3]);
+            *reinterpret_cast<float4*>(sj + ofs(lrow, c + 4, np, 4)) = make_float4(v[4], v[5], v[6], v[7]);
+          }
+        }
+      }
+      fence_before();
+      __syncthreads();
+      if (j == L - 2) {
+        jet_fwd_rows<BF16>(P1, opA, G, np, true);   // last hidden layer: FP32 rows in P1
+      } else if (X3) {
+        jet_fwd_rows<BF16>(P1, opA, G, np, true, true);
+        zero_rows<BF16>(opA, R, np, ES);
+        __syncthreads();
+        alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
+      } else {
+        jet_fwd_rows<BF16>(P1, opA, G, np, false);
+        zero_rows<BF16>(opA, R, np, ES);
+      }
+      cx.publish();
+    }
+
+    // ---- output layer (H_{L-1} as FP32 rows in P1)
+    {
+      const int K = A.width[L - 1];
+      const float* Wl = prm + A.w_off[L - 1];
+      const float* bl = prm + A.b_off[L - 1];
+      for (int e = tid; e < RMAX * d_out; e += NTC) {
+        const int r = e % RMAX, o = e / RMAX;
+        float z = 0.f;
+        const float* w = &Wl[(int64_t)o * K];
+        for (int k = 0; k < K; k += 4) {
+          const float4 hv = ld4(&P1[r * LDS + k]);
+          z = fmaf(hv.x, __ldg(&w[k]), z);
+          z = fmaf(hv.y, __ldg(&w[k + 1]), z);
+          z = fmaf(hv.z, __ldg(&w[k + 2]), z);
+          z = fmaf(hv.w, __ldg(&w[k + 3]), z);
+        }
+        if (row_v[r]) z += __ldg(&bl[o]);
+        ybuf[r * MAX_OUT + o] = z;
+        gybuf[r * MAX_OUT + o] = 0.f;
+      }
+    }
+    __syncthreads();
+
+    // ---- operator program: term values per (point, term), outputs and squared errors per
+    // (point, output), the loss seeds, then the program adjoint per (point, term). Scratch lives in
+    // opB, which no MMA reads between the last forward GEMM and the first backward bulk copy.
+    const int n_out = G.n_outputs;
+    {
+      float* tv = reinterpret_cast<float*>(opB);           // [MAX_TERMS][T] term values
+      float* seedv = tv + MAX_TERMS * RMAX;                 // [MAX_OUT][T] dL/d(output)
+      double* e2 = reinterpret_cast<double*>(seedv + MAX_OUT * RMAX);   // [MAX_OUT][T]
+      const int nt = G.n_terms;
+      for (int e = tid; e < T * nt; e += NTC) {
+        const int p = e % T, t = e / T;
+        const DevTerm& tm = G.terms[t];
+        const bool valid = p < nvalid;
+        const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+        float prod = 1.f;
+        for (int f = 0; f < tm.n_factors; ++f) {
+          const DevFactor& fc = G.factors[tm.factor_first + f];
+          float F = 0.f;
+          for (int u = 0; u < fc.n_parts; ++u) {
+            const DevPart& pt = G.parts[fc.part_first + u];
+            F = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, F);
+          }
+          prod *= powf_(F, fc.power);
+        }
+        tv[t * RMAX + p] = c * prod;
+      }
+      __syncthreads();
+      for (int e = tid; e < T * n_out; e += NTC) {
+        const int p = e % T, o = e / T;
+        const bool valid = p < nvalid;
+        float out = 0.f;
+        for (int t = 0; t < nt; ++t)
+          if (G.terms[t].output == o) out += tv[t * RMAX + p];
+        const float tgt = (G.target_array >= 0 && valid)
+                              ? A.arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
+        const float err = valid ? out - tgt : 0.f;
+        e2[o * RMAX + p] = (double)err * (double)err;
+        seedv[o * RMAX + p] = err * G.seed_scale[o];
+        if (A.outputs && G.out_offset >= 0 && valid)
+          A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = out;
+      }
+      __syncthreads();
+      if (tid < n_out) {   // fixed-order FP64 sum over the tile's points
+        double sum = 0.0;
+        for (int p = 0; p < T; ++p) sum += e2[tid * RMAX + p];
+        cur_slot[tid] += sum;
+      }
+      if (A.do_grad) {
+        for (int e = tid; e < T * nt; e += NTC) {
+          const int p = e % T, t = e / T;
+          const DevTerm& tm = G.terms[t];
+          const bool valid = p < nvalid;
+          const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+          const float dt = seedv[tm.output * RMAX + p] * c;
+          if (dt == 0.f) continue;
+          float F[MAX_TERM_FACTORS];
+          for (int f = 0; f < tm.n_factors; ++f) {
+            const DevFactor& fc = G.factors[tm.factor_first + f];
+            float v = 0.f;
+            for (int u = 0; u < fc.n_parts; ++u) {
+              const DevPart& pt = G.parts[fc.part_first + u];
+              v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
+            }
+            F[f] = v;
+          }
+          for (int f = 0; f < tm.n_factors; ++f) {
+            const DevFactor& fc = G.factors[tm.factor_first + f];
+            float d = dt * dpowf_(F[f], fc.power);
+            for (int g = 0; g < tm.n_factors; ++g)
+              if (g != f) d *= powf_(F[g], G.factors[tm.factor_first + g].power);
+            for (int u = 0; u < fc.n_parts; ++u) {
+              const DevPart& pt = G.parts[fc.part_first + u];
+              atomicAdd(&gybuf[(pt.stream * T + p) * MAX_OUT + fc.var], d * pt.weight);
+            }
+          }
+        }
+      }
+    }
+    if (!A.do_grad) continue;
+    cx.publish();   // the program's scratch in opB is dead: Z_{L-1} overlaps the output layer
+    cx.issue(opB, scr + (int64_t)(L - 2) * scr_slot, (uint32_t)(128 * p16(A.width[L - 1]) * 4));
+
+    float* grad = A.partial + (int64_t)tile.seg * A.part_stride;
+    const bool first = tile.first_in_seg != 0;
+    // ---- output layer backward: dW, db (H_{L-1} in P1), then dL/dH_{L-1} -> P1
+    {
+      const int K = A.width[L - 1], kp = p16(K);
+      const float* Wl = prm + A.w_off[L - 1];
+      float* dW = grad + A.w_off[L - 1];
+      float* db = grad + A.b_off[L - 1];
+      for (int e = tid; e < d_out * K; e += NTC) {
+        const int o = e / K, k = e - o * K;
+        float sum = 0.f;
+        for (int r = 0; r < R; ++r) sum = fmaf(gybuf[r * MAX_OUT + o], P1[r * LDS + k], sum);
+        dW[(int64_t)o * K + k] = first ? sum : dW[(int64_t)o * K + k] + sum;
+      }
+      for (int o = tid; o < d_out; o += NTC) {
+        float sum = 0.f;
+        for (int r = 0; r < R; ++r)
+          if (row_v[r]) sum += gybuf[r * MAX_OUT + o];
+        db[o] = first ? sum : db[o] + sum;
+      }
+      __syncthreads();
+      for (int e = tid; e < RMAX * (kp >> 2); e += NTC) {
+        const int r = e % RMAX, k = (e / RMAX) * 4;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (r < R)
+          for (int o = 0; o < d_out; ++o) {
+            const float g = gybuf[r * MAX_OUT + o];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (k + i < K) v[i] = fmaf(g, __ldg(&Wl[(int64_t)o * K + k + i]), v[i]);
+          }
+        st4(&P1[r * LDS + k], make_float4(v[0], v[1], v[2], v[3]));
+      }
+    }
+    __syncthreads();
+
+    for (int l = L - 1; l >= 1; --l) {
+      const int N = A.width[l], np = p16(N);
+      if (l >= 2 && tid == 0)   // warm L2 with the pre-activations the dW operand will need
+        prefetch_l2(scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * p16(A.width[l - 1]) * 4));
+      // Z_l (scratch slot l-1, interleaved FP32) -> opB, issued ahead
+      cx.ensure(opB, scr + (int64_t)(l - 1) * scr_slot, (uint32_t)(128 * np * 4));
+      // jet adjoint: P1 (dL/dH_l) -> P1 (dL/dZ_l) in place, streams of a site in increasing order;
+      // also the K-major operand copy of dL/dZ_l in opA for the dX GEMM
+      {
+        const int n4s = np >> 2;
+        for (int q = 0; q < G.n_sites; ++q) {
+          const int ns = G.site_nstreams[q];
+          const int base = G.site_streams[q][0];
+          if (with_class(G.site_cls[q], [&](auto cc) {
+                for (int e = tid; e < T * n4s; e += NTC)
+                  jet_bwd_cls<decltype(cc)::value, BF16>(P1, opB, opA, T, base, e % T, (e / T) * 4, np,
+                                                         l >= 2);
+              }))
+            continue;
+          for (int e = tid; e < T * n4s; e += NTC) {
+            const int p = e % T, n = (e / T) * 4;
+            Sig sg;
+            sg.make(ld4o(opB, ofs(base * T + p, n, np, 4)), true);
+            for (int m = 0; m < ns; ++m) {
+              const int b = G.site_streams[q][m];
+              float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+              const int pf = G.st_pull_first[b];
+              for (int u = 0; u < G.st_npull[b]; ++u) {
+                const DevPull& pl = G.pulls[pf + u];
+                float4 v = f4mul(ld4(&P1[(pl.alpha * T + p) * LDS + n]),
+                                 f4scale(sg.sel(pl.kk), (float)pl.mult));
+                for (int f = 0; f < pl.n_oth; ++f) v = f4mul(v, ld4o(opB, ofs(pl.oth[f] * T + p, n, np, 4)));
+                acc = f4add(acc, v);
+              }
+              const float4 gz = acc;
+              st4(&P1[(b * T + p) * LDS + n], gz);
+              if (l >= 2) put4<BF16>(opA, b * T + p, n, np, gz);
+            }
+          }
+        }
+      }
+      if (l == 1) {
+        __syncthreads();
+        // input layer gradients from dL/dZ_1 in P1: 4 row quarters per neuron, then reduced
+        float* red = reinterpret_cast<float*>(opA);   // [4][640] partials; opA is free at layer 1
+        {
+          const int n = tid & 127, part = tid >> 7;
+          float sb = 0.f;
+          float sw[TDG_MAX_DIN] = {0.f, 0.f, 0.f, 0.f};
+          if (n < N)
+            for (int r = 32 * part; r < 32 * part + 32 && r < R; ++r) {
+              const int sr = row_s[r];
+              const int o = G.st_order[sr];
+              const float g = P1[r * LDS + n];
+              if (o == 0) {
+                sb += g;
+#pragma unroll
+                for (int a = 0; a < TDG_MAX_DIN; ++a)
+                  if (a < d_in) sw[a] = fmaf(g, xsbuf[r * TDG_MAX_DIN + a], sw[a]);
+              } else if (o == 1) {
+                const int ax = G.st_axis[sr];
+#pragma unroll
+                for (int a = 0; a < TDG_MAX_DIN; ++a)
+                  if (a == ax) sw[a] += g;
+              }
+            }
+          red[part * 640 + n] = sb;
+#pragma unroll
+          for (int a = 0; a < TDG_MAX_DIN; ++a) red[part * 640 + 128 * (1 + a) + n] = sw[a];
+        }
+        __syncthreads();
+        float* dW0 = grad + A.w_off[0];
+        float* db0 = grad + A.b_off[0];
+        for (int e = tid; e < N * (1 + d_in); e += NTC) {
+          const int n = e % N, c = e / N;   // c = 0: bias, c = 1 + a: weight column a
+          const float v = red[128 * c + n] + red[640 + 128 * c + n] + red[1280 + 128 * c + n] +
+                          red[1920 + 128 * c + n];
+          float* dst = c == 0 ? &db0[n] : &dW0[n * d_in + (c - 1)];
+          *dst = first ? v : *dst + v;
+        }
+        break;
+      }
+      const int K = A.width[l - 1], kp = p16(K);
+      zero_rows<BF16>(opA, R, np, ES);
+      if (X3) {
+        __syncthreads();
+        alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
+      }
+      cx.publish();
+      // dX: D1[rows x kp] = dL/dZ_l[rows x np] . (W_{l-1}^T packed [kp x np])^T
+      if (X3) {
+        gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wbwd_off[l - 1], kp, np);
+      } else {
+        cx.load(opB, TA.wpack + TA.wbwd_off[l - 1], (uint32_t)(kp * np * ES));
+        gemm_issue<BF16>(D1, opA, opB, kp, np, cx.bar_mma);
+        cx.wait_mma();
+      }
+      // dW operand A = dL/dZ_l^T [128 (neurons, zero padded) x 128 rows] from P1, and the bias
+      // gradient of Linear l-1 (sum of dL/dZ_l over value rows) from the same reads
+      {
+        float* red = ybuf;   // [4][128] bias partials
+        const int n = tid & 127;
+        float sb = 0.f;
+        for (int e = tid; e < 128 * 32; e += NTC) {
+          const int r = (e >> 7) * 4;
+          float v[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            v[i] = (n < N && r + i < R) ? P1[(r + i) * LDS + n] : 0.f;
+            if (row_v[r + i]) sb += v[i];
+          }
+          put4<BF16>(opA, n, r, 128, make_float4(v[0], v[1], v[2], v[3]));
+          if (X3)   // lane = neuron n, columns = rows r..r+3 (the same r for the whole warp)
+            tmem_st4(ALO + lane_addr + r, v[0] - to_tf32(v[0]), v[1] - to_tf32(v[1]),
+                     v[2] - to_tf32(v[2]), v[3] - to_tf32(v[3]));
+        }
+        if (X3) tmem_st_wait();
+        red[(tid >> 7) * 128 + n] = sb;
+        __syncthreads();
+        float* db = grad + A.b_off[l - 1];
+        for (int m = tid; m < N; m += NTC) {
+          const float v = red[m] + red[128 + m] + red[256 + m] + red[384 + m];
+          db[m] = first ? v : db[m] + v;
+        }
+      }
+      cx.publish();
+      // Z_{l-1} (scratch slot l-2, interleaved FP32) -> P1 region by bulk copy
+      unsigned char* zst = reinterpret_cast<unsigned char*>(P1);
+      cx.load(zst, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));
+      // H_{l-1}^T [kp x 128 rows] -> opB. Lanes take consecutive rows (conflict-free reads of the
+      // interleaved Z), 4 neurons each; each quad of lanes then transposes its 4 x 4 block with
+      // shuffles so that a lane stores one neuron for 4 consecutive rows.
+      if (X3) {
+        // split TF32: two halves of 64 rows, [hi | lo] of H_{l-1}^T for the half in opB, then
+        // hi*hi + hi*lo + lo*hi per K-step (A lo = dL/dZ_l^T low part in tensor memory)
+        const uint32_t lo_off = (uint32_t)kp * 64 * 4;
+        const uint32_t idesc = instr_desc<false>(128, kp);
+        for (int hh = 0; hh < 2; ++hh) {
+          auto build = [&](auto hrow) {
+            for (int e = tid; e < 16 * kp; e += NTC) {
+              const int r = 64 * hh + (e & 63), n = (e >> 6) * 4;
+              float o[4];
+              quad_transpose(hrow(r, n), lane, o);
+              const int qd = lane & 3, rl = (r & ~3) - 64 * hh;
+              put4<false>(opB, n + qd, rl, 64, make_float4(o[0], o[1], o[2], o[3]));
+              put4<false>(opB + lo_off, n + qd, rl, 64,
+                          make_float4(o[0] - to_tf32(o[0]), o[1] - to_tf32(o[1]),
+                                      o[2] - to_tf32(o[2]), o[3] - to_tf32(o[3])));
+            }
+          };
+          if (!with_class(G.grp_cls, [&](auto cc) {
+                build([&](int r, int n) { return h_row_c<decltype(cc)::value>(G, zst, kp, row_s, row_p, r, n); });
+              }))
+            build([&](int r, int n) { return h_row(G, zst, kp, row_s, row_p, r, n); });
+          cx.publish();
+          if (tid == 0) {
+            const uint32_t a0 = smem_u32(opA), b0 = smem_u32(opB);
+            for (int j = 0; j < 8; ++j) {
+              const int kk = 64 * hh + 8 * j;
+              const uint64_t ad = smem_desc(a0 + (kk / 8) * 256, 128, 4096);
+              const uint64_t bh = smem_desc(b0 + j * 256, 128, 2048);
+              const uint64_t bl = smem_desc(b0 + lo_off + j * 256, 128, 2048);
+              mma<false>(D2, ad, bh, idesc, hh > 0 || j > 0);
+              mma<false>(D2, ad, bl, idesc, true);
+              mma_ts_tf32(D2, ALO + kk, bh, idesc, true);
+            }
+            commit(cx.bar_mma);
+          }
+          cx.wait_mma();
+        }
+        cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
+        d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);
+      } else {
+        auto build = [&](auto hrow) {
+          for (int e = tid; e < 32 * kp; e += NTC) {
+            const int r = e & 127, n = (e >> 7) * 4;
+            float o[4];
+            quad_transpose(hrow(r, n), lane, o);
+            put4<BF16>(opB, n + (lane & 3), r & ~3, 128, make_float4(o[0], o[1], o[2], o[3]));
+          }
+        };
+        if (!with_class(G.grp_cls, [&](auto cc) {
+              build([&](int r, int n) { return h_row_c<decltype(cc)::value>(G, zst, kp, row_s, row_p, r, n); });
+            }))
+          build([&](int r, int n) { return h_row(G, zst, kp, row_s, row_p, r, n); });
+        cx.publish();
+        // dW: D2[128 x kp] = A[128 x 128] . B[kp x 128]^T
+        gemm_issue<BF16>(D2, opA, opB, kp, 128, cx.bar_mma);
+        d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);   // overlaps the dW MMA
+        cx.wait_mma();
+        cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
+      }
+      // flush dW_{l-1} (TMEM lane = output neuron, columns = input neurons) with vector atomic
+      // adds into this CTA's zeroed gradient segment; one thread owns each address, so the
+      // accumulation order is fixed
+      {
+        float* dW = grad + A.w_off[l - 1];
+        for (int c = 8 * cgrp; c < kp; c += 32) {
+          float v[8];
+          tmem_ld8(D2 + lane_addr + c, v);
+          if (lrow < N) {
+            if (c < K) red_add4(&dW[(int64_t)lrow * K + c], v[0], v[1], v[2], v[3]);
+            if (c + 4 < K) red_add4(&dW[(int64_t)lrow * K + c + 4], v[4], v[5], v[6], v[7]);
+          }
+        }
+      }
+      fence_before();
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  if (cur_group >= 0 && tid < Gs->n_outputs)
+    A.slot_partial[(int64_t)cta * A.n_slots + Gs->slot_first + tid] += cur_slot[tid];
+  fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(*tmem_slot, X3 ? 512 : 256);
+}
+
+// ---- weight packing: every hidden Linear j into forward (N x K) and transposed (K x N) operands.
+// Split TF32 packs each operand as two K-halves, each a [hi | lo] pair of K-major blocks.
+namespace {
+template <bool BF16, bool X3>
+__global__ void pack_weights_kernel(const float* __restrict__ params, TcLaunch t) {
+  constexpr int ES = BF16 ? 2 : 4;
+  const int j = blockIdx.y + 1;   // hidden Linear layers 1..n_layers-2
+  const int K = t.width[j], N = t.width[j + 1];
+  const int kp = p16(K), np = p16(N);
+  const float* W = params + t.w_off[j];
+  unsigned char* f = t.wpack + t.fwd_off[j];
+  unsigned char* b = t.wpack + t.bwd_off[j];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < np * kp; e += gridDim.x * blockDim.x) {
+    const int n = e / kp, k = e % kp;
+    const float v = (n < N && k < K) ? W[(int64_t)n * K + k] : 0.f;
+    if (X3) {
+      const float hi = to_tf32(v), lo = to_tf32(v - hi);
+      const int kh = kp / 2, nh = np / 2;
+      // forward operand [np x kp], halves over k
+      {
+        const int h = k / kh, kk = k - h * kh;
+        unsigned char* base = f + (size_t)h * 2 * np * kh * 4;
+        *reinterpret_cast<float*>(base + ofs(n, kk, kh, 4)) = hi;
+        *reinterpret_cast<float*>(base + (size_t)np * kh * 4 + ofs(n, kk, kh, 4)) = lo;
+      }
+      // transposed operand [kp x np], halves over n
+      {
+        const int h = n / nh, nn = n - h * nh;
+        unsigned char* base = b + (size_t)h * 2 * kp * nh * 4;
+        *reinterpret_cast<float*>(base + ofs(k, nn, nh, 4)) = hi;
+        *reinterpret_cast<float*>(base + (size_t)kp * nh * 4 + ofs(k, nn, nh, 4)) = lo;
+      }
+    } else {
+      put<BF16>(f, ofs(n, k, kp, ES), v);
+      put<BF16>(b, ofs(k, n, np, ES), v);
+    }
+  }
+}
+
+template <bool BF16, bool X3>
+cudaError_t launch_variant(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
+  static bool attr = false;
+  const size_t smem = fused_tc_smem_bytes();
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(fused_tc_kernel<BF16, X3>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (a.n_layers > 2) {   // pack this step's hidden weights
+    pack_weights_kernel<BF16, X3><<<dim3(16, a.n_layers - 2), 256, 0, s>>>(a.params, t);
+    count_launch();
+  }
+  TcArgs ta{};
+  ta.wpack = t.wpack;
+  for (int l = 0; l < TDG_MAX_LAYERS; ++l) { ta.wfwd_off[l] = t.fwd_off[l]; ta.wbwd_off[l] = t.bwd_off[l]; }
+  ta.err = t.err;
+  fused_tc_kernel<BF16, X3><<<n_ctas, NTC, smem, s>>>(a, ta);
+  count_launch();
+  return cudaGetLastError();
+}
+}  // namespace
+
+}  // namespace tdg

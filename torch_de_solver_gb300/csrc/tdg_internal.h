@@ -53,13 +53,15 @@ struct DevPart {
 struct alignas(16) DevGroup {
   int32_t n_rows, T, S, n_sites;
   int32_t n_outputs, n_terms, problem, slot_first;
-  int32_t target_array, pad0;
+  int32_t target_array;
+  int32_t grp_cls;                        // the jet class shared by every site of the group, else -1
   int64_t out_offset;
   float seed_scale[MAX_OUT];              // 2 * loss weight of each output's slot
   int32_t site_points[MAX_SITES];
   float site_off[MAX_SITES][TDG_MAX_DIN];
   int8_t site_nstreams[MAX_SITES];
   int8_t site_streams[MAX_SITES][SMAX];   // row-stream indices of a site, increasing order; [0] = value
+  int8_t site_cls[MAX_SITES];             // compile-time jet class of a site (tdg_jetcls.h), -1: tables
   int8_t st_site[SMAX], st_order[SMAX], st_axis[SMAX], st_nrule[SMAX];
   int8_t st_npull[SMAX];
   int16_t st_pull_first[SMAX];
@@ -150,6 +152,9 @@ struct PlainArgs {
 };
 cudaError_t run_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
+cudaError_t launch_tc_tf32(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
+cudaError_t launch_tc_bf16(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
+cudaError_t launch_tc_3x(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
 cudaError_t launch_bounded_wait_selftest(int max_polls, int* gave_up, cudaStream_t s);
 cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
                                const int32_t* seg_list, int n_problems, int64_t n_params,

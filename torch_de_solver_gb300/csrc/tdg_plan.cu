@@ -5,12 +5,14 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
 #include <vector>
 
 #include "tdg_internal.h"
+#include "tdg_jetcls.h"
 
 namespace tdg {
 
@@ -143,8 +145,36 @@ void free_plan(tdg_plan* p) {
 }
 
 // Build the DevGroup of one group description.
+// Compile-time jet class of the site whose streams are rows [base, base + ns): the class with the
+// same stream list whose folded rules equal the tables just built, else -1 (table-driven code).
+int site_class(const DevGroup& G, const std::vector<Key>& keys, int base, int ns) {
+  if (ns > jetcls::CS) return -1;
+  int ord[jetcls::CS] = {0};
+  int ax[jetcls::CS][3] = {{0}};
+  for (int m = 0; m < ns; ++m) {
+    const Key& k = keys[base + m];
+    ord[m] = (int)k.size();
+    for (size_t i = 0; i < k.size(); ++i) ax[m][i] = k[i];
+  }
+  const int c = jetcls::classify(ns, ord, ax);
+  if (c < 0) return -1;
+  const jetcls::Rules R = jetcls::make_rules(jetcls::kSiteClasses[c]);
+  if (R.ns != ns) return -1;
+  for (int m = 1; m < ns; ++m) {
+    const int s = base + m;
+    if (R.nrule[m] != G.st_nrule[s]) return -1;
+    for (int u = 0; u < R.nrule[m]; ++u) {
+      const DevRule& r = G.rules[s][u];
+      if (r.k != R.k[m][u] || r.mult != R.mult[m][u]) return -1;
+      for (int i = 0; i < r.k; ++i)
+        if (r.sub[i] != base + R.sub[m][u][i]) return -1;
+    }
+  }
+  return c;
+}
+
 tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d_in, int d_out,
-                       DevGroup& G, int& S_out) {
+                       bool tables_only, DevGroup& G, int& S_out) {
   memset(&G, 0, sizeof(G));
   if (g.n_sites < 1 || g.n_sites > MAX_SITES) return fail(TDG_ERR_UNSUPPORTED, "group has %d sites (1..%d)", g.n_sites, MAX_SITES);
   if (g.site_first < 0 || g.site_first + g.n_sites > d.n_sites) return fail(TDG_ERR_INVALID, "site range out of bounds");
@@ -219,8 +249,12 @@ tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d
         for (int i = 0; i < rules[u].k; ++i) G.rules[s][u].sub[i] = (int8_t)rules[u].sub[i];
       }
     }
+    G.site_cls[q] = (int8_t)(tables_only ? -1 : site_class(G, keys, S, st.n_streams));
     S += st.n_streams;
   }
+  G.grp_cls = G.site_cls[0];
+  for (int q = 1; q < g.n_sites; ++q)
+    if (G.site_cls[q] != G.grp_cls) G.grp_cls = -1;
   // adjoint pull lists: for each stream beta, every (alpha, rule) term whose derivative wrt Z[beta]
   // is nonzero. Pulls for beta are stored contiguously.
   std::vector<std::vector<DevPull>> pulls(S);
@@ -323,6 +357,20 @@ int32_t tdg_abi_version(void) { return TDG_ABI_VERSION; }
 const char* tdg_last_error(void) { return g_error.c_str(); }
 int64_t tdg_launch_count(void) { return g_launches.load(); }
 
+int32_t tdg_site_class(int32_t n_streams, const tdg_stream_desc* streams) {
+  if (n_streams < 1 || n_streams > jetcls::CS || !streams) return -1;
+  int ord[jetcls::CS] = {0};
+  int ax[jetcls::CS][3] = {{0}};
+  for (int m = 0; m < n_streams; ++m) {
+    if (streams[m].order < 0 || streams[m].order > TDG_MAX_ORDER) return -1;
+    ord[m] = streams[m].order;
+    for (int i = 0; i < ord[m]; ++i) ax[m][i] = streams[m].axes[i];
+    std::sort(ax[m], ax[m] + ord[m]);
+  }
+  const int c = jetcls::classify(n_streams, ord, ax);
+  return c >= 0 && jetcls::make_rules(jetcls::kSiteClasses[c]).ns == n_streams ? c : -1;
+}
+
 tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
   if (!desc || !out) return fail(TDG_ERR_INVALID, "null argument");
   *out = nullptr;
@@ -369,6 +417,9 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
   p->arrays.assign(d.arrays, d.arrays + d.n_arrays);
   p->array_len.assign(d.array_len, d.array_len + d.n_arrays);
 
+  // TDG_JET_TABLES=1 runs every site through the table-driven jet code (to compare both codes)
+  const char* jt = std::getenv("TDG_JET_TABLES");
+  const bool tables_only = jt && jt[0] == '1';
   std::vector<DevGroup> groups(d.n_groups);
   std::vector<DevTile> tiles;
   double hidden_pairs = 0, all_pairs = 0;
@@ -378,7 +429,7 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     const tdg_group_desc& g = d.groups[gi];
     if (g.problem < 0 || g.problem >= d.n_problems) { free_plan(p); return fail(TDG_ERR_INVALID, "group problem out of range"); }
     int S = 0;
-    tdg_status st = build_group(d, g, d_in, d_out, groups[gi], S);
+    tdg_status st = build_group(d, g, d_in, d_out, tables_only, groups[gi], S);
     if (st != TDG_OK) { free_plan(p); return st; }
     p->max_streams = std::max(p->max_streams, S);
     p->ginfo.push_back(HostGroupInfo{g.n_rows, S, g.problem});

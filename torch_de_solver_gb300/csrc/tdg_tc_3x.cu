@@ -1,0 +1,10 @@
+// The split TF32 (3xTF32) variant of the tensor-core fused kernel.
+#include "tdg_fused_tc.cuh"
+
+namespace tdg {
+
+cudaError_t launch_tc_3x(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
+  return launch_variant<false, true>(a, t, n_ctas, s);
+}
+
+}  // namespace tdg

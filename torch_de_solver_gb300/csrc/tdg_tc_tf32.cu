@@ -1,0 +1,10 @@
+// The TF32 variant of the tensor-core fused kernel.
+#include "tdg_fused_tc.cuh"
+
+namespace tdg {
+
+cudaError_t launch_tc_tf32(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
+  return launch_variant<false, false>(a, t, n_ctas, s);
+}
+
+}  // namespace tdg
