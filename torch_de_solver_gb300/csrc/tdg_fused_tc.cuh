@@ -114,8 +114,17 @@ struct TcCtx {
     ph_tma ^= 1;
     inflight = false;
   }
-  // every thread: generic-proxy smem writes visible to the tensor cores, then barrier
+  // every thread: generic-proxy shared-memory accesses ordered before the async proxy's (MMA
+  // operand reads, bulk copies into shared memory), then barrier
   __device__ __forceinline__ void publish() {
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+  }
+  // as publish, for global memory too: the saved pre-activations (generic stores) before the
+  // bulk copies that read them back
+  __device__ __forceinline__ void publish_global() {
     fence_async_all();
     fence_before();
     __syncthreads();
@@ -746,7 +755,8 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
     }
     if (!A.do_grad) continue;
-    cx.publish();   // the program's scratch in opB is dead: Z_{L-1} overlaps the output layer
+    cx.publish_global();   // opB's program scratch is dead and every Z of the tile stored:
+                           // Z_{L-1} overlaps the output layer
     cx.issue(opB, scr + (int64_t)(L - 2) * scr_slot, (uint32_t)(128 * p16(A.width[L - 1]) * 4));
 
     float* grad = A.partial + (int64_t)tile.seg * A.part_stride;
