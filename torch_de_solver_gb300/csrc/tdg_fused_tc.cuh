@@ -199,15 +199,6 @@ __device__ void gemm3x(TcCtx& cx, uint32_t d, const unsigned char* a, uint32_t a
 template <int C>
 __host__ __device__ constexpr jetcls::Rules rules_of() { return jetcls::make_rules(jetcls::kSiteClasses[C]); }
 
-// whether a rule of stream M reads the pre-activation of stream Q (Q may be M itself)
-template <int C>
-__host__ __device__ constexpr bool reads_sub(int M, int Q) {
-  bool r = false;
-  for (int u = 0; u < rules_of<C>().nrule[M]; ++u)
-    for (int i = 0; i < rules_of<C>().k[M][u]; ++i) r = r || rules_of<C>().sub[M][u][i] == Q;
-  return r;
-}
-
 template <typename F, int... I>
 __device__ __forceinline__ void sfor_(F& f, std::integer_sequence<int, I...>) {
   (f(std::integral_constant<int, I>{}), ...);
@@ -310,29 +301,93 @@ __device__ __forceinline__ void jet_bwd_cls(float* __restrict__ P1, const unsign
   });
 }
 
-// forward jet of stream m of one site for one (stream, point) row, from interleaved FP32 Z rows
-template <int C>
-__device__ __forceinline__ float4 h_row_cls(const unsigned char* __restrict__ zst, int kp, int T, int base,
-                                            int m, int p, int n) {
+// H of every stream of a classed site at (point p, neurons n..n+3) from interleaved FP32 Z rows;
+// f(m, h) receives the site's stream m, m ascending
+template <int C, typename F>
+__device__ __forceinline__ void site_values_cls(const unsigned char* __restrict__ zs, int kp, int T, int base,
+                                                int p, int n, F&& f) {
   constexpr int NS = rules_of<C>().ns;
-  Sig sg;
-  sg.make(ld4o(zst, ofs(base * T + p, n, kp, 4)), false);
-  float4 h = sg.t;
+  float4 z[NS];
   sfor<NS>([&](auto mc) {
     constexpr int M = decltype(mc)::value;
-    if constexpr (M >= 1) {
-      if (m == M) {
-        float4 z[NS];
-        sfor<NS>([&](auto sc) {
-          constexpr int Q = decltype(sc)::value;
-          if constexpr (reads_sub<C>(M, Q)) z[Q] = ld4o(zst, ofs((base + Q) * T + p, n, kp, 4));
-          else z[Q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        });
-        h = cls_rule_sum<C, M>(sg, z);
+    z[M] = ld4o(zs, ofs((base + M) * T + p, n, kp, 4));
+  });
+  Sig sg;
+  sg.make(z[0], rules_of<C>().maxk >= 4);
+  sfor<NS>([&](auto mc) {
+    constexpr int M = decltype(mc)::value;
+    if constexpr (M == 0) f(0, sg.t);
+    else f(M, cls_rule_sum<C, M>(sg, z));
+  });
+}
+
+// the same for a site run through the rule tables
+template <typename F>
+__device__ __forceinline__ void site_values_tab(const DevGroup& G, int q, const unsigned char* __restrict__ zs,
+                                                int kp, int p, int n, F&& f) {
+  const int T = G.T, ns = G.site_nstreams[q], base = G.site_streams[q][0];
+  Sig sg;
+  sg.make(ld4o(zs, ofs(base * T + p, n, kp, 4)), false);
+  for (int m = 0; m < ns; ++m) {
+    const int s = base + m;
+    float4 h = sg.t;
+    if (m > 0) {
+      h = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int u = 0; u < G.st_nrule[s]; ++u) {
+        const DevRule& ru = G.rules[s][u];
+        float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
+        for (int i = 0; i < ru.k; ++i) v = f4mul(v, ld4o(zs, ofs(ru.sub[i] * T + p, n, kp, 4)));
+        h = f4add(h, v);
       }
     }
-  });
-  return h;
+    f(m, h);
+  }
+}
+
+// thread (p, 4 neurons): H of every (stream, point) row from interleaved FP32 pre-activations zs
+// (kp per row) into FP32 rows of P (stride LDS); tanh once per (point, neuron)
+__device__ void jet_rows_from_op(const unsigned char* __restrict__ zs, float* __restrict__ P,
+                                 const DevGroup& G, int kp) {
+  const int T = G.T, n4s = kp >> 2;
+  for (int q = 0; q < G.n_sites; ++q) {
+    const int base = G.site_streams[q][0];
+    if (with_class(G.site_cls[q], [&](auto cc) {
+          for (int e = threadIdx.x; e < T * n4s; e += NTC) {
+            const int p = e % T, n = (e / T) * 4;
+            site_values_cls<decltype(cc)::value>(zs, kp, T, base, p, n, [&](int m, float4 h) {
+              st4(&P[((base + m) * T + p) * LDS + n], h);
+            });
+          }
+        }))
+      continue;
+    for (int e = threadIdx.x; e < T * n4s; e += NTC) {
+      const int p = e % T, n = (e / T) * 4;
+      site_values_tab(G, q, zs, kp, p, n,
+                      [&](int m, float4 h) { st4(&P[((base + m) * T + p) * LDS + n], h); });
+    }
+  }
+}
+
+// rows [r_lo, r_lo + nr) of FP32 rows P (kp neurons) transposed into the K-major operand dst
+// (operand rows = neurons, K = the nr rows); rows >= R read as zero. A warp reads 32 neurons of
+// one row (conflict-free) and a lane stores 4 rows of its neuron. Split TF32 stores [hi | lo].
+template <bool BF16, bool X3>
+__device__ void rows_to_opT(const float* __restrict__ P, unsigned char* __restrict__ dst, int kp, int r_lo,
+                            int nr, int R, uint32_t lo_off) {
+  for (int e = threadIdx.x; e < kp * (nr >> 2); e += NTC) {
+    const int n = e % kp, rl = 4 * (e / kp), r = r_lo + rl;
+    float v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = r + i < R ? P[(r + i) * LDS + n] : 0.f;
+    if (X3) {
+      put4<false>(dst, n, rl, nr, make_float4(v[0], v[1], v[2], v[3]));
+      put4<false>(dst + lo_off, n, rl, nr,
+                  make_float4(v[0] - to_tf32(v[0]), v[1] - to_tf32(v[1]), v[2] - to_tf32(v[2]),
+                              v[3] - to_tf32(v[3])));
+    } else {
+      put4<BF16>(dst, n, rl, nr, make_float4(v[0], v[1], v[2], v[3]));
+    }
+  }
 }
 
 // thread (p, 4 neurons): tanh jet of every stream of point p from plain Z rows in P, written as
@@ -390,52 +445,6 @@ __device__ void alo_from_rows(const float* __restrict__ P, uint32_t a_lo, int kp
   tmem_st_wait();
 }
 
-// tanh jet of one (stream, point) row for 4 neurons from interleaved FP32 pre-activations
-__device__ __forceinline__ float4 h_row(const DevGroup& G, const unsigned char* __restrict__ zst, int kp,
-                                        const int8_t* row_s, const uint8_t* row_p, int r, int n) {
-  float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
-  const int sr = row_s[r];
-  if (sr < 0) return h;
-  const int T = G.T, p = row_p[r], q = G.st_site[sr];
-  Sig sg;
-  sg.make(ld4o(zst, ofs(G.site_streams[q][0] * T + p, n, kp, 4)), false);
-  if (G.st_order[sr] == 0) return sg.t;
-  for (int u = 0; u < G.st_nrule[sr]; ++u) {
-    const DevRule& ru = G.rules[sr][u];
-    float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
-    for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4o(zst, ofs(ru.sub[f] * T + p, n, kp, 4)));
-    h = f4add(h, v);
-  }
-  return h;
-}
-
-// h_row for a group whose sites all have compile-time class C
-template <int C>
-__device__ __forceinline__ float4 h_row_c(const DevGroup& G, const unsigned char* __restrict__ zst, int kp,
-                                          const int8_t* row_s, const uint8_t* row_p, int r, int n) {
-  const int sr = row_s[r];
-  if (sr < 0) return make_float4(0.f, 0.f, 0.f, 0.f);
-  const int base = G.site_streams[G.st_site[sr]][0];
-  return h_row_cls<C>(zst, kp, G.T, base, sr - base, row_p[r], n);
-}
-
-// 4 x 4 transpose inside each quad of lanes: lane (base + i) holds values for 4 neurons of row
-// (base + i); afterwards o[j] is neuron (i) of row (base + j). All 32 lanes must participate.
-__device__ __forceinline__ void quad_transpose(float4 h, int lane, float (&o)[4]) {
-  const int qd = lane & 3, qbase = lane & ~3;
-  o[0] = o[1] = o[2] = o[3] = 0.f;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int si = (qd - k) & 3;
-    const float send = si == 0 ? h.x : si == 1 ? h.y : si == 2 ? h.z : h.w;
-    const float got = __shfl_sync(0xffffffffu, send, qbase | ((qd + k) & 3));
-    const int di = (qd + k) & 3;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      if (di == j) o[j] = got;
-  }
-}
-
 // dL/dH rows from the dX accumulator (tensor memory) into plain FP32 rows, zero past K and R
 __device__ __forceinline__ void d1_to_rows(uint32_t d1, float* __restrict__ P, int kp, int K, int R,
                                            uint32_t lane_addr, int lrow, int cgrp) {
@@ -486,8 +495,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   uint64_t* bars = reinterpret_cast<uint64_t*>(wred + (NTC / 32) * MAX_OUT);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
   int8_t* row_s = reinterpret_cast<int8_t*>(tmem_slot + 4);     // [128] stream of a row, -1 padding
-  uint8_t* row_p = reinterpret_cast<uint8_t*>(row_s + 128);     // [128] point of a row
-  uint8_t* row_v = row_p + 128;                                  // [128] 1 on value-stream rows
+  uint8_t* row_v = reinterpret_cast<uint8_t*>(row_s + 128);     // [128] 1 on value-stream rows
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int cta = blockIdx.x;
@@ -540,7 +548,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const int T0 = Gs->T, R0 = Gs->T * Gs->S;
         const int sr = tid < R0 ? tid / T0 : -1;
         row_s[tid] = (int8_t)sr;
-        row_p[tid] = (uint8_t)(tid < R0 ? tid - sr * T0 : 0);
         row_v[tid] = (uint8_t)(sr >= 0 && Gs->st_order[sr] == 0);
       }
       __syncthreads();
@@ -892,6 +899,8 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         gemm_issue<BF16>(D1, opA, opB, kp, np, cx.bar_mma);
         cx.wait_mma();
       }
+      // opB is free: Z_{l-1} (scratch slot l-2, interleaved FP32) overlaps the dW operand A build
+      cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));
       // dW operand A = dL/dZ_l^T [128 (neurons, zero padded) x 128 rows] from P1, and the bias
       // gradient of Linear l-1 (sum of dL/dZ_l over value rows) from the same reads
       {
@@ -921,34 +930,18 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         }
       }
       cx.publish();
-      // Z_{l-1} (scratch slot l-2, interleaved FP32) -> P1 region by bulk copy
-      unsigned char* zst = reinterpret_cast<unsigned char*>(P1);
-      cx.load(zst, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));
-      // H_{l-1}^T [kp x 128 rows] -> opB. Lanes take consecutive rows (conflict-free reads of the
-      // interleaved Z), 4 neurons each; each quad of lanes then transposes its 4 x 4 block with
-      // shuffles so that a lane stores one neuron for 4 consecutive rows.
+      // H_{l-1}: the tanh jets of Z_{l-1} (opB) per (point, 4 neurons), every stream of a site
+      // at once, as FP32 rows in P1 (dL/dZ_l there is consumed)
+      cx.wait_tma();
+      jet_rows_from_op(opB, P1, G, kp);
+      cx.publish();
       if (X3) {
         // split TF32: two halves of 64 rows, [hi | lo] of H_{l-1}^T for the half in opB, then
         // hi*hi + hi*lo + lo*hi per K-step (A lo = dL/dZ_l^T low part in tensor memory)
         const uint32_t lo_off = (uint32_t)kp * 64 * 4;
         const uint32_t idesc = instr_desc<false>(128, kp);
         for (int hh = 0; hh < 2; ++hh) {
-          auto build = [&](auto hrow) {
-            for (int e = tid; e < 16 * kp; e += NTC) {
-              const int r = 64 * hh + (e & 63), n = (e >> 6) * 4;
-              float o[4];
-              quad_transpose(hrow(r, n), lane, o);
-              const int qd = lane & 3, rl = (r & ~3) - 64 * hh;
-              put4<false>(opB, n + qd, rl, 64, make_float4(o[0], o[1], o[2], o[3]));
-              put4<false>(opB + lo_off, n + qd, rl, 64,
-                          make_float4(o[0] - to_tf32(o[0]), o[1] - to_tf32(o[1]),
-                                      o[2] - to_tf32(o[2]), o[3] - to_tf32(o[3])));
-            }
-          };
-          if (!with_class(G.grp_cls, [&](auto cc) {
-                build([&](int r, int n) { return h_row_c<decltype(cc)::value>(G, zst, kp, row_s, row_p, r, n); });
-              }))
-            build([&](int r, int n) { return h_row(G, zst, kp, row_s, row_p, r, n); });
+          rows_to_opT<false, true>(P1, opB, kp, 64 * hh, 64, R, lo_off);
           cx.publish();
           if (tid == 0) {
             const uint32_t a0 = smem_u32(opA), b0 = smem_u32(opB);
@@ -968,18 +961,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
         d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);
       } else {
-        auto build = [&](auto hrow) {
-          for (int e = tid; e < 32 * kp; e += NTC) {
-            const int r = e & 127, n = (e >> 7) * 4;
-            float o[4];
-            quad_transpose(hrow(r, n), lane, o);
-            put4<BF16>(opB, n + (lane & 3), r & ~3, 128, make_float4(o[0], o[1], o[2], o[3]));
-          }
-        };
-        if (!with_class(G.grp_cls, [&](auto cc) {
-              build([&](int r, int n) { return h_row_c<decltype(cc)::value>(G, zst, kp, row_s, row_p, r, n); });
-            }))
-          build([&](int r, int n) { return h_row(G, zst, kp, row_s, row_p, r, n); });
+        rows_to_opT<BF16, false>(P1, opB, kp, 0, 128, R, 0);
         cx.publish();
         // dW: D2[128 x kp] = A[128 x 128] . B[kp x 128]^T
         gemm_issue<BF16>(D2, opA, opB, kp, 128, cx.bar_mma);

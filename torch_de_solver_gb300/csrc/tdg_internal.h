@@ -53,8 +53,7 @@ struct DevPart {
 struct alignas(16) DevGroup {
   int32_t n_rows, T, S, n_sites;
   int32_t n_outputs, n_terms, problem, slot_first;
-  int32_t target_array;
-  int32_t grp_cls;                        // the jet class shared by every site of the group, else -1
+  int32_t target_array, pad0;
   int64_t out_offset;
   float seed_scale[MAX_OUT];              // 2 * loss weight of each output's slot
   int32_t site_points[MAX_SITES];

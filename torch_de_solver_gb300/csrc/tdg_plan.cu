@@ -252,9 +252,6 @@ tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d
     G.site_cls[q] = (int8_t)(tables_only ? -1 : site_class(G, keys, S, st.n_streams));
     S += st.n_streams;
   }
-  G.grp_cls = G.site_cls[0];
-  for (int q = 1; q < g.n_sites; ++q)
-    if (G.site_cls[q] != G.grp_cls) G.grp_cls = -1;
   // adjoint pull lists: for each stream beta, every (alpha, rule) term whose derivative wrt Z[beta]
   // is nonzero. Pulls for beta are stored contiguously.
   std::vector<std::vector<DevPull>> pulls(S);
