@@ -969,19 +969,27 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         cx.wait_mma();
         cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
       }
-      // flush dW_{l-1} (TMEM lane = output neuron, columns = input neurons) with vector atomic
-      // adds into this CTA's zeroed gradient segment; one thread owns each address, so the
-      // accumulation order is fixed
+      // flush dW_{l-1} (TMEM lane = output neuron, columns = input neurons) into this CTA's zeroed
+      // gradient segment: staged in opA (free after the dW MMAs) as 128 rows of 32 16-byte
+      // chunks, chunk j of row n at j ^ (n & 7) (conflict-free writes and reads), then every warp
+      // adds whole rows with coalesced vector atomics. One thread owns each address in every
+      // tile, so the accumulation order is fixed.
       {
-        float* dW = grad + A.w_off[l - 1];
+        float4* stage = reinterpret_cast<float4*>(opA);
         for (int c = 8 * cgrp; c < kp; c += 32) {
           float v[8];
           tmem_ld8(D2 + lane_addr + c, v);
-          if (lrow < N) {
-            if (c < K) red_add4(&dW[(int64_t)lrow * K + c], v[0], v[1], v[2], v[3]);
-            if (c + 4 < K) red_add4(&dW[(int64_t)lrow * K + c + 4], v[4], v[5], v[6], v[7]);
-          }
+          const int j = c >> 2, sw = lrow & 7;
+          stage[lrow * 32 + (j ^ sw)] = make_float4(v[0], v[1], v[2], v[3]);
+          stage[lrow * 32 + ((j + 1) ^ sw)] = make_float4(v[4], v[5], v[6], v[7]);
         }
+        __syncthreads();
+        float* dW = grad + A.w_off[l - 1];
+        for (int n = warp; n < N; n += NTC / 32)
+          if (4 * lane < K) {
+            const float4 v = stage[n * 32 + (lane ^ (n & 7))];
+            red_add4(&dW[(int64_t)n * K + 4 * lane], v.x, v.y, v.z, v.w);
+          }
       }
       fence_before();
       __syncthreads();
