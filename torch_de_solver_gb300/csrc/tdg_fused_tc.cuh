@@ -28,6 +28,14 @@ using namespace tc;
 
 constexpr int OPB = 128 * 128 * 4;    // bytes of one operand buffer
 constexpr int NTC = 512;              // threads of the tensor-core kernel (16 warps)
+// the small parameters of the current problem, staged in shared memory when the problem changes:
+// hidden biases (128 per hidden Linear), W0 and b0 of the input layer, W and b of the output layer
+constexpr int PB_HB = 0;
+constexpr int PB_W0 = PB_HB + (TDG_MAX_LAYERS - 2) * TDG_MAX_WIDTH;
+constexpr int PB_B0 = PB_W0 + TDG_MAX_WIDTH * TDG_MAX_DIN;
+constexpr int PB_WL = PB_B0 + TDG_MAX_WIDTH;
+constexpr int PB_BL = PB_WL + TDG_MAX_DOUT * TDG_MAX_WIDTH;
+constexpr int PBUF = PB_BL + TDG_MAX_DOUT;
 
 __device__ __forceinline__ int p16(int w) { return (w + 15) & ~15; }
 
@@ -489,7 +497,8 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   float* ybuf = P1 + RMAX * LDS;
   float* gybuf = ybuf + RMAX * MAX_OUT;
   float* xsbuf = gybuf + RMAX * MAX_OUT;
-  DevGroup* Gs = reinterpret_cast<DevGroup*>(xsbuf + RMAX * TDG_MAX_DIN);
+  float* pbuf = xsbuf + RMAX * TDG_MAX_DIN;                     // PBUF floats: small parameters
+  DevGroup* Gs = reinterpret_cast<DevGroup*>(pbuf + PBUF);
   double* cur_slot = reinterpret_cast<double*>(Gs + 1);        // [MAX_OUT]
   double* wred = cur_slot + MAX_OUT;                           // [NTC/32][MAX_OUT]
   uint64_t* bars = reinterpret_cast<uint64_t*>(wred + (NTC / 32) * MAX_OUT);
@@ -522,7 +531,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   const int lrow = 32 * (warp & 3) + lane;
   const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
   const int cgrp = warp >> 2;                    // 0..3: this warp's 8-column chunks c = 8*cgrp + 32*i
-  int cur_group = -1;
+  int cur_group = -1, cur_problem = -1;
   // the first bulk copy of hidden GEMM j's forward weights (split TF32: the first [hi | lo] half)
   auto wfwd_first = [&](int j) {
     const uint32_t nk = (uint32_t)p16(A.width[j + 1]) * p16(A.width[j]);
@@ -550,12 +559,21 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         row_s[tid] = (int8_t)sr;
         row_v[tid] = (uint8_t)(sr >= 0 && Gs->st_order[sr] == 0);
       }
+      if (Gs->problem != cur_problem) {   // stage the problem's small parameters
+        cur_problem = Gs->problem;
+        const float* pp = A.params + (int64_t)cur_problem * A.n_params;
+        for (int j = 1; j < L - 1; ++j)
+          for (int n = tid; n < A.width[j + 1]; n += NTC) pbuf[PB_HB + (j - 1) * TDG_MAX_WIDTH + n] = pp[A.b_off[j] + n];
+        for (int e = tid; e < A.width[1] * d_in; e += NTC) pbuf[PB_W0 + e] = pp[A.w_off[0] + e];
+        for (int n = tid; n < A.width[1]; n += NTC) pbuf[PB_B0 + n] = pp[A.b_off[0] + n];
+        for (int e = tid; e < d_out * A.width[L - 1]; e += NTC) pbuf[PB_WL + e] = pp[A.w_off[L - 1] + e];
+        for (int o = tid; o < d_out; o += NTC) pbuf[PB_BL + o] = pp[A.b_off[L - 1] + o];
+      }
       __syncthreads();
     }
     const DevGroup& G = *Gs;
     const int T = G.T, S = G.S, R = T * S;
     const int nvalid = tile.nvalid, row0 = tile.row0;
-    const float* prm = A.params + (int64_t)G.problem * A.n_params;
 
     for (int e = tid; e < RMAX * d_in; e += NTC) {
       const int r = e / d_in, a = e - r * d_in;
@@ -571,8 +589,8 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     // ---- input layer -> Z_1 (plain in P1, interleaved FP32 in scratch slot 0)
     {
       const int N = A.width[1], np = p16(N);
-      const float* W0 = prm + A.w_off[0];
-      const float* b0 = prm + A.b_off[0];
+      const float* W0 = pbuf + PB_W0;
+      const float* b0 = pbuf + PB_B0;
       for (int e = tid; e < RMAX * (np >> 2); e += NTC) {
         const int r = e % RMAX, n = (e / RMAX) * 4;
         float z[4] = {0.f, 0.f, 0.f, 0.f};
@@ -584,10 +602,10 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             if (nn >= N) continue;
             if (o == 0) {
               float v = 0.f;
-              for (int a = 0; a < d_in; ++a) v = fmaf(__ldg(&W0[nn * d_in + a]), xsbuf[r * TDG_MAX_DIN + a], v);
-              z[i] = v + __ldg(&b0[nn]);
+              for (int a = 0; a < d_in; ++a) v = fmaf(W0[nn * d_in + a], xsbuf[r * TDG_MAX_DIN + a], v);
+              z[i] = v + b0[nn];
             } else if (o == 1) {
-              z[i] = __ldg(&W0[nn * d_in + G.st_axis[s]]);
+              z[i] = W0[nn * d_in + G.st_axis[s]];
             }
           }
         }
@@ -624,7 +642,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       if (j + 1 < L - 1) wfwd_first(j + 1);   // opB is free: overlaps the epilogue and the jets
       // epilogue: D1 -> +bias -> P1 (plain) and scratch slot j (interleaved FP32)
       {
-        const float* bj = prm + A.b_off[j];
+        const float* bj = pbuf + PB_HB + (j - 1) * TDG_MAX_WIDTH;
         const bool val = row_v[lrow] != 0;
         unsigned char* sj = reinterpret_cast<unsigned char*>(scr + (int64_t)j * scr_slot);
         for (int c = 8 * cgrp; c < np; c += 32) {
@@ -633,7 +651,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             const int n = c + i;
-            v[i] = n < N ? v[i] + (val ? __ldg(&bj[n]) : 0.f) : 0.f;
+            v[i] = n < N ? v[i] + (val ? bj[n] : 0.f) : 0.f;
             if (lrow >= R) v[i] = 0.f;
           }
           st4(&P1[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
@@ -663,20 +681,20 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     // ---- output layer (H_{L-1} as FP32 rows in P1)
     {
       const int K = A.width[L - 1];
-      const float* Wl = prm + A.w_off[L - 1];
-      const float* bl = prm + A.b_off[L - 1];
+      const float* Wl = pbuf + PB_WL;
+      const float* bl = pbuf + PB_BL;
       for (int e = tid; e < RMAX * d_out; e += NTC) {
         const int r = e % RMAX, o = e / RMAX;
         float z = 0.f;
         const float* w = &Wl[(int64_t)o * K];
         for (int k = 0; k < K; k += 4) {
           const float4 hv = ld4(&P1[r * LDS + k]);
-          z = fmaf(hv.x, __ldg(&w[k]), z);
-          z = fmaf(hv.y, __ldg(&w[k + 1]), z);
-          z = fmaf(hv.z, __ldg(&w[k + 2]), z);
-          z = fmaf(hv.w, __ldg(&w[k + 3]), z);
+          z = fmaf(hv.x, w[k], z);
+          z = fmaf(hv.y, w[k + 1], z);
+          z = fmaf(hv.z, w[k + 2], z);
+          z = fmaf(hv.w, w[k + 3], z);
         }
-        if (row_v[r]) z += __ldg(&bl[o]);
+        if (row_v[r]) z += bl[o];
         ybuf[r * MAX_OUT + o] = z;
         gybuf[r * MAX_OUT + o] = 0.f;
       }
@@ -771,7 +789,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     // ---- output layer backward: dW, db (H_{L-1} in P1), then dL/dH_{L-1} -> P1
     {
       const int K = A.width[L - 1], kp = p16(K);
-      const float* Wl = prm + A.w_off[L - 1];
+      const float* Wl = pbuf + PB_WL;
       float* dW = grad + A.w_off[L - 1];
       float* db = grad + A.b_off[L - 1];
       for (int e = tid; e < d_out * K; e += NTC) {
@@ -795,7 +813,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             const float g = gybuf[r * MAX_OUT + o];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
-              if (k + i < K) v[i] = fmaf(g, __ldg(&Wl[(int64_t)o * K + k + i]), v[i]);
+              if (k + i < K) v[i] = fmaf(g, Wl[o * K + k + i], v[i]);
           }
         st4(&P1[r * LDS + k], make_float4(v[0], v[1], v[2], v[3]));
       }
