@@ -224,6 +224,15 @@ __device__ __forceinline__ bool with_class(int cls, F&& f) {
   return done;
 }
 
+// f(T) with the points per tile T a compile-time constant when the group is a single site of
+// class C (then T = 128 / streams), else the group's runtime T
+template <int C, typename F>
+__device__ __forceinline__ void with_tile_points(const DevGroup& G, F&& f) {
+  constexpr int TC = RMAX / rules_of<C>().ns;
+  if (G.n_sites == 1 && G.T == TC) f(std::integral_constant<int, TC>{});
+  else f(G.T);
+}
+
 // H_M = sum_u mult * tanh^(k)(z_0) * prod Z[sub]  (same operation order as the table rules)
 template <int C, int M, int NS>
 __device__ __forceinline__ float4 cls_rule_sum(const Sig& sg, const float4 (&z)[NS]) {
@@ -360,12 +369,15 @@ __device__ void jet_rows_from_op(const unsigned char* __restrict__ zs, float* __
   for (int q = 0; q < G.n_sites; ++q) {
     const int base = G.site_streams[q][0];
     if (with_class(G.site_cls[q], [&](auto cc) {
-          for (int e = threadIdx.x; e < T * n4s; e += NTC) {
-            const int p = e % T, n = (e / T) * 4;
-            site_values_cls<decltype(cc)::value>(zs, kp, T, base, p, n, [&](int m, float4 h) {
-              st4(&P[((base + m) * T + p) * LDS + n], h);
-            });
-          }
+          with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
+            const int Tc = tq;
+            for (int e = threadIdx.x; e < Tc * n4s; e += NTC) {
+              const int p = e % Tc, n = (e / Tc) * 4;
+              site_values_cls<decltype(cc)::value>(zs, kp, Tc, base, p, n, [&](int m, float4 h) {
+                st4(&P[((base + m) * Tc + p) * LDS + n], h);
+              });
+            }
+          });
         }))
       continue;
     for (int e = threadIdx.x; e < T * n4s; e += NTC) {
@@ -411,9 +423,12 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
     const int base = G.site_streams[q][0];
     // classed site: one loop per class, the dispatch outside it
     if (with_class(G.site_cls[q], [&](auto cc) {
-          for (int e = threadIdx.x; e < T * n4s; e += NTC)
-            jet_fwd_cls<decltype(cc)::value, BF16>(P, out, T, base, e % T, (e / T) * 4, np, inplace,
-                                                   !inplace || also_out);
+          with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
+            const int Tc = tq;
+            for (int e = threadIdx.x; e < Tc * n4s; e += NTC)
+              jet_fwd_cls<decltype(cc)::value, BF16>(P, out, Tc, base, e % Tc, (e / Tc) * 4, np, inplace,
+                                                     !inplace || also_out);
+          });
         }))
       continue;
     for (int e = threadIdx.x; e < T * n4s; e += NTC) {
@@ -505,6 +520,8 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
   int8_t* row_s = reinterpret_cast<int8_t*>(tmem_slot + 4);     // [128] stream of a row, -1 padding
   uint8_t* row_v = reinterpret_cast<uint8_t*>(row_s + 128);     // [128] 1 on value-stream rows
+  int8_t* row_ax = reinterpret_cast<int8_t*>(row_v + 128);      // [128] -1 value row, axis of a first
+                                                                 // derivative row, -2 otherwise
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int cta = blockIdx.x;
@@ -558,6 +575,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const int sr = tid < R0 ? tid / T0 : -1;
         row_s[tid] = (int8_t)sr;
         row_v[tid] = (uint8_t)(sr >= 0 && Gs->st_order[sr] == 0);
+        row_ax[tid] = (int8_t)(sr < 0 ? -2 : Gs->st_order[sr] == 0 ? -1 : Gs->st_order[sr] == 1 ? Gs->st_axis[sr] : -2);
       }
       if (Gs->problem != cur_problem) {   // stage the problem's small parameters
         cur_problem = Gs->problem;
@@ -593,20 +611,18 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const float* b0 = pbuf + PB_B0;
       for (int e = tid; e < RMAX * (np >> 2); e += NTC) {
         const int r = e % RMAX, n = (e / RMAX) * 4;
+        const int ax = row_ax[r];   // a value row: W0 x + b0; d/dx_a: column a of W0; else 0
         float z[4] = {0.f, 0.f, 0.f, 0.f};
-        if (r < R) {
-          const int s = r / T, o = G.st_order[s];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const int nn = n + i;
-            if (nn >= N) continue;
-            if (o == 0) {
-              float v = 0.f;
-              for (int a = 0; a < d_in; ++a) v = fmaf(W0[nn * d_in + a], xsbuf[r * TDG_MAX_DIN + a], v);
-              z[i] = v + b0[nn];
-            } else if (o == 1) {
-              z[i] = W0[nn * d_in + G.st_axis[s]];
-            }
+        for (int i = 0; i < 4; ++i) {
+          const int nn = n + i;
+          if (nn >= N) continue;
+          if (ax == -1) {
+            float v = 0.f;
+            for (int a = 0; a < d_in; ++a) v = fmaf(W0[nn * d_in + a], xsbuf[r * TDG_MAX_DIN + a], v);
+            z[i] = v + b0[nn];
+          } else if (ax >= 0) {
+            z[i] = W0[nn * d_in + ax];
           }
         }
         const float4 zv = make_float4(z[0], z[1], z[2], z[3]);
@@ -648,10 +664,12 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         for (int c = 8 * cgrp; c < np; c += 32) {
           float v[8];
           tmem_ld8(D1 + lane_addr + c, v);
+          const float4 b0v = ld4(&bj[c]), b1v = ld4(&bj[c + 4]);
+          const float bb[8] = {b0v.x, b0v.y, b0v.z, b0v.w, b1v.x, b1v.y, b1v.z, b1v.w};
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             const int n = c + i;
-            v[i] = n < N ? v[i] + (val ? bj[n] : 0.f) : 0.f;
+            v[i] = n < N ? v[i] + (val ? bb[i] : 0.f) : 0.f;
             if (lrow >= R) v[i] = 0.f;
           }
           st4(&P1[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
@@ -834,9 +852,12 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           const int ns = G.site_nstreams[q];
           const int base = G.site_streams[q][0];
           if (with_class(G.site_cls[q], [&](auto cc) {
-                for (int e = tid; e < T * n4s; e += NTC)
-                  jet_bwd_cls<decltype(cc)::value, BF16>(P1, opB, opA, T, base, e % T, (e / T) * 4, np,
-                                                         l >= 2);
+                with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
+                  const int Tc = tq;
+                  for (int e = tid; e < Tc * n4s; e += NTC)
+                    jet_bwd_cls<decltype(cc)::value, BF16>(P1, opB, opA, Tc, base, e % Tc, (e / Tc) * 4, np,
+                                                           l >= 2);
+                });
               }))
             continue;
           for (int e = tid; e < T * n4s; e += NTC) {
