@@ -196,7 +196,7 @@ def read_traffic(tag):
     if not os.path.exists(path):
         return None
     for ln in open(path):
-        if ln.startswith('dram_bytes_per_point:'):
+        if ln.strip().startswith('dram_bytes_per_point:'):
             return float(ln.split(':')[1])
     return None
 
@@ -365,7 +365,8 @@ def run_ours(args, rank, world):
     flops = plan.info.flops_hidden
     kern_s = statistics.mean(kern_ms) / 1e3
     achieved = flops / kern_s / 1e12
-    peak = bf16 / 2.0   # dense TF32 tensor rate = half the measured dense BF16 rate
+    # dense TF32 tensor rate = half the measured dense BF16 rate
+    peak = bf16 if args.precision == 'bf16' else bf16 / 2.0
     tag = f'{args.form}_{args.precision}_{args.workload}'
     tpp = read_traffic(tag)
     roofline = {'bound': 'tensor', 'achieved': round(achieved, 3), 'peak': round(peak, 1),
@@ -376,8 +377,8 @@ def run_ours(args, rank, world):
                 if args.form == 'fused' else 'plain form: all per-layer launches of the step',
                 'kernel_ms': round(statistics.mean(kern_ms), 4),
                 'algorithmic_flops_per_launch': flops,
-                'peak_source': 'MEASURED_PEAKS.json bf16_tflops / 2 (dense TF32 = half of BF16)'
-                if peaks else 'fallback 1.9 PFLOP/s bf16 / 2'}
+                'peak_source': ('MEASURED_PEAKS.json bf16_tflops' if peaks else 'fallback 1.9 PFLOP/s bf16')
+                + ('' if args.precision == 'bf16' else ' / 2 (dense TF32 = half of BF16)')}
     line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
             'steps_per_s': round(1e3 / ms_per_step, 3), 'higher_is_better': True,

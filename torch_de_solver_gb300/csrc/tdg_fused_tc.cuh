@@ -62,7 +62,11 @@ __device__ __forceinline__ float4 f4scale(float4 a, float c) { return make_float
 struct Sig {   // tanh and its derivatives, as functions of t = tanh(z), for 4 neurons
   float4 t, s1, s2, s3, s4;
   __device__ __forceinline__ void make(const float4 z, bool need4) {
-    t = make_float4(tanhf(z.x), tanhf(z.y), tanhf(z.z), tanhf(z.w));
+    from_t(make_float4(tanhf(z.x), tanhf(z.y), tanhf(z.z), tanhf(z.w)), need4);
+  }
+  // from t = tanh(z) saved by the forward pass
+  __device__ __forceinline__ void from_t(const float4 tv, bool need4) {
+    t = tv;
     const float4 tt = f4mul(t, t);
     s1 = make_float4(1.f - tt.x, 1.f - tt.y, 1.f - tt.z, 1.f - tt.w);
     s2 = f4scale(f4mul(t, s1), -2.f);
@@ -251,7 +255,8 @@ __device__ __forceinline__ float4 cls_rule_sum(const Sig& sg, const float4 (&z)[
 // and/or operand rows of `out`)
 template <int C, bool BF16>
 __device__ __forceinline__ void jet_fwd_cls(float* __restrict__ P, unsigned char* __restrict__ out, int T,
-                                            int base, int p, int n, int np, bool inplace, bool write_out) {
+                                            int base, int p, int n, int np, bool inplace, bool write_out,
+                                            unsigned char* __restrict__ tsave) {
   constexpr int NS = rules_of<C>().ns;
   float4 z[NS];
   sfor<NS>([&](auto mc) {
@@ -260,6 +265,7 @@ __device__ __forceinline__ void jet_fwd_cls(float* __restrict__ P, unsigned char
   });
   Sig sg;
   sg.make(z[0], rules_of<C>().maxk >= 4);
+  if (tsave) *reinterpret_cast<float4*>(tsave + ofs(base * T + p, n, np, 4)) = sg.t;
   sfor<NS>([&](auto mc) {
     constexpr int M = decltype(mc)::value;
     float4 h;
@@ -286,7 +292,7 @@ __device__ __forceinline__ void jet_bwd_cls(float* __restrict__ P1, const unsign
     gz[M] = make_float4(0.f, 0.f, 0.f, 0.f);
   });
   Sig sg;
-  sg.make(z[0], rules_of<C>().maxk + 1 >= 4);
+  sg.from_t(z[0], rules_of<C>().maxk + 1 >= 4);   // the value row holds t = tanh(z)
   gz[0] = f4mul(g[0], sg.s1);
   sfor<NS>([&](auto mc) {
     constexpr int M = decltype(mc)::value;
@@ -330,7 +336,7 @@ __device__ __forceinline__ void site_values_cls(const unsigned char* __restrict_
     z[M] = ld4o(zs, ofs((base + M) * T + p, n, kp, 4));
   });
   Sig sg;
-  sg.make(z[0], rules_of<C>().maxk >= 4);
+  sg.from_t(z[0], rules_of<C>().maxk >= 4);   // the value row holds t = tanh(z)
   sfor<NS>([&](auto mc) {
     constexpr int M = decltype(mc)::value;
     if constexpr (M == 0) f(0, sg.t);
@@ -344,7 +350,7 @@ __device__ __forceinline__ void site_values_tab(const DevGroup& G, int q, const 
                                                 int kp, int p, int n, F&& f) {
   const int T = G.T, ns = G.site_nstreams[q], base = G.site_streams[q][0];
   Sig sg;
-  sg.make(ld4o(zs, ofs(base * T + p, n, kp, 4)), false);
+  sg.from_t(ld4o(zs, ofs(base * T + p, n, kp, 4)), false);   // the value row holds t = tanh(z)
   for (int m = 0; m < ns; ++m) {
     const int s = base + m;
     float4 h = sg.t;
@@ -413,9 +419,12 @@ __device__ void rows_to_opT(const float* __restrict__ P, unsigned char* __restri
 // thread (p, 4 neurons): tanh jet of every stream of point p from plain Z rows in P, written as
 // operand rows of `out`, or, when `inplace`, back into P as FP32 rows (streams of a site from the
 // highest order down, the value stream last, so every Z a rule reads is still intact).
+// When tsave is given, t = tanh(z) of every value row is also stored there (the saved
+// pre-activations of the layer, interleaved FP32), for the backward pass.
 template <bool BF16>
 __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ out,
-                             const DevGroup& G, int np, bool inplace, bool also_out = false) {
+                             const DevGroup& G, int np, bool inplace, bool also_out,
+                             unsigned char* __restrict__ tsave) {
   const int T = G.T;
   const int n4s = np >> 2;
   for (int q = 0; q < G.n_sites; ++q) {
@@ -427,7 +436,7 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
             const int Tc = tq;
             for (int e = threadIdx.x; e < Tc * n4s; e += NTC)
               jet_fwd_cls<decltype(cc)::value, BF16>(P, out, Tc, base, e % Tc, (e / Tc) * 4, np, inplace,
-                                                     !inplace || also_out);
+                                                     !inplace || also_out, tsave);
           });
         }))
       continue;
@@ -435,6 +444,7 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
       const int p = e % T, n = (e / T) * 4;
       Sig sg;
       sg.make(ld4(&P[(base * T + p) * LDS + n]), false);
+      if (tsave) *reinterpret_cast<float4*>(tsave + ofs(base * T + p, n, np, 4)) = sg.t;
       for (int m = ns - 1; m >= 0; --m) {
         const int s = G.site_streams[q][m];
         float4 h = sg.t;
@@ -627,19 +637,21 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         }
         const float4 zv = make_float4(z[0], z[1], z[2], z[3]);
         st4(&P1[r * LDS + n], zv);
-        if (A.do_grad) *reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(scr) + ofs(r, n, np, 4)) = zv;
+        if (A.do_grad && ax != -1)   // value rows: the jets save t = tanh(z) instead
+          *reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(scr) + ofs(r, n, np, 4)) = zv;
       }
     }
     __syncthreads();
+    unsigned char* t0 = A.do_grad ? reinterpret_cast<unsigned char*>(scr) : nullptr;
     if (L == 2) {
-      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true);   // last hidden layer: FP32 rows in P1
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true, false, t0);   // last hidden layer: rows in P1
     } else if (X3) {
-      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true, true);
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true, true, t0);
       zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
       __syncthreads();
       alo_from_rows(P1, ALO, p16(A.width[1]), lane_addr, lrow, cgrp);
     } else {
-      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), false);
+      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), false, false, t0);
       zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
     }
     cx.publish();
@@ -674,7 +686,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           }
           st4(&P1[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
           st4(&P1[lrow * LDS + c + 4], make_float4(v[4], v[5], v[6], v[7]));
-          if (A.do_grad) {
+          if (A.do_grad && !val) {   // value rows: the jets save t = tanh(z) instead
             *reinterpret_cast<float4*>(sj + ofs(lrow, c, np, 4)) = make_float4(v[0], v[1], v[2], v[3]);
             *reinterpret_cast<float4*>(sj + ofs(lrow, c + 4, np, 4)) = make_float4(v[4], v[5], v[6], v[7]);
           }
@@ -682,15 +694,16 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
       fence_before();
       __syncthreads();
+      unsigned char* tj = A.do_grad ? reinterpret_cast<unsigned char*>(scr + (int64_t)j * scr_slot) : nullptr;
       if (j == L - 2) {
-        jet_fwd_rows<BF16>(P1, opA, G, np, true);   // last hidden layer: FP32 rows in P1
+        jet_fwd_rows<BF16>(P1, opA, G, np, true, false, tj);   // last hidden layer: FP32 rows in P1
       } else if (X3) {
-        jet_fwd_rows<BF16>(P1, opA, G, np, true, true);
+        jet_fwd_rows<BF16>(P1, opA, G, np, true, true, tj);
         zero_rows<BF16>(opA, R, np, ES);
         __syncthreads();
         alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
       } else {
-        jet_fwd_rows<BF16>(P1, opA, G, np, false);
+        jet_fwd_rows<BF16>(P1, opA, G, np, false, false, tj);
         zero_rows<BF16>(opA, R, np, ES);
       }
       cx.publish();
@@ -863,7 +876,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           for (int e = tid; e < T * n4s; e += NTC) {
             const int p = e % T, n = (e / T) * 4;
             Sig sg;
-            sg.make(ld4o(opB, ofs(base * T + p, n, np, 4)), true);
+            sg.from_t(ld4o(opB, ofs(base * T + p, n, np, 4)), true);   // the value row holds t
             for (int m = 0; m < ns; ++m) {
               const int b = G.site_streams[q][m];
               float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
