@@ -143,9 +143,9 @@ __device__ __forceinline__ void red_add4(float* dst, float a, float b, float c, 
 }
 
 __device__ __forceinline__ float to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+  // round to the nearest TF32 value (10 explicit mantissa bits), ties away from zero: add half a
+  // TF32 unit in the last place to the magnitude bits, then clear the 13 low mantissa bits
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
 }
 
 // store a value into an operand buffer as TF32 (rounded) or BF16
