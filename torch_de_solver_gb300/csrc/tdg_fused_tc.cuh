@@ -27,7 +27,9 @@ namespace {
 using namespace tc;
 
 constexpr int OPB = 128 * 128 * 4;    // bytes of one operand buffer
-constexpr int NTC = 512;              // threads of the tensor-core kernel (16 warps)
+constexpr int NTC = 512;              // threads of the tensor-core kernel (a multiple of 128)
+constexpr int NCG = NTC / 128;        // TMEM column groups: warps sharing one lane quarter
+constexpr int NPART = NTC / 128;      // row parts of the per-neuron reductions (128 threads each)
 // the small parameters of the current problem, staged in shared memory when the problem changes:
 // hidden biases (128 per hidden Linear), W0 and b0 of the input layer, W and b of the output layer
 constexpr int PB_HB = 0;
@@ -468,7 +470,7 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
 // columns [0, kp) at a_lo. Each warp writes its own lane quarter, columns split over 4 warps.
 __device__ void alo_from_rows(const float* __restrict__ P, uint32_t a_lo, int kp, uint32_t lane_addr,
                               int lrow, int cgrp) {
-  for (int c = 8 * cgrp; c < kp; c += 32) {
+  for (int c = 8 * cgrp; c < kp; c += 8 * NCG) {
     const float4 x0 = ld4(&P[lrow * LDS + c]), x1 = ld4(&P[lrow * LDS + c + 4]);
     const float v[8] = {x0.x - to_tf32(x0.x), x0.y - to_tf32(x0.y), x0.z - to_tf32(x0.z),
                         x0.w - to_tf32(x0.w), x1.x - to_tf32(x1.x), x1.y - to_tf32(x1.y),
@@ -481,7 +483,7 @@ __device__ void alo_from_rows(const float* __restrict__ P, uint32_t a_lo, int kp
 // dL/dH rows from the dX accumulator (tensor memory) into plain FP32 rows, zero past K and R
 __device__ __forceinline__ void d1_to_rows(uint32_t d1, float* __restrict__ P, int kp, int K, int R,
                                            uint32_t lane_addr, int lrow, int cgrp) {
-  for (int c = 8 * cgrp; c < kp; c += 32) {
+  for (int c = 8 * cgrp; c < kp; c += 8 * NCG) {
     float v[8];
     tmem_ld8(d1 + lane_addr + c, v);
 #pragma unroll
@@ -557,7 +559,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   // TMEM lane quarter and column group of this warp in the epilogues
   const int lrow = 32 * (warp & 3) + lane;
   const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
-  const int cgrp = warp >> 2;                    // 0..3: this warp's 8-column chunks c = 8*cgrp + 32*i
+  const int cgrp = warp >> 2;                    // this warp's 8-column chunks c = 8 * (cgrp + NCG * i)
   int cur_group = -1, cur_problem = -1;
   // the first bulk copy of hidden GEMM j's forward weights (split TF32: the first [hi | lo] half)
   auto wfwd_first = [&](int j) {
@@ -673,7 +675,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const float* bj = pbuf + PB_HB + (j - 1) * TDG_MAX_WIDTH;
         const bool val = row_v[lrow] != 0;
         unsigned char* sj = reinterpret_cast<unsigned char*>(scr + (int64_t)j * scr_slot);
-        for (int c = 8 * cgrp; c < np; c += 32) {
+        for (int c = 8 * cgrp; c < np; c += 8 * NCG) {
           float v[8];
           tmem_ld8(D1 + lane_addr + c, v);
           const float4 b0v = ld4(&bj[c]), b1v = ld4(&bj[c + 4]);
@@ -898,23 +900,22 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       if (l == 1) {
         __syncthreads();
         // input layer gradients from dL/dZ_1 in P1: 4 row quarters per neuron, then reduced
-        float* red = reinterpret_cast<float*>(opA);   // [4][640] partials; opA is free at layer 1
+        float* red = reinterpret_cast<float*>(opA);   // [NPART][640] partials; opA is free at layer 1
         {
+          constexpr int RPP = (RMAX + NPART - 1) / NPART;   // rows per part
           const int n = tid & 127, part = tid >> 7;
           float sb = 0.f;
           float sw[TDG_MAX_DIN] = {0.f, 0.f, 0.f, 0.f};
           if (n < N)
-            for (int r = 32 * part; r < 32 * part + 32 && r < R; ++r) {
-              const int sr = row_s[r];
-              const int o = G.st_order[sr];
+            for (int r = RPP * part; r < RPP * part + RPP && r < R; ++r) {
+              const int ax = row_ax[r];   // -1 value row, else the axis of a first derivative
               const float g = P1[r * LDS + n];
-              if (o == 0) {
+              if (ax == -1) {
                 sb += g;
 #pragma unroll
                 for (int a = 0; a < TDG_MAX_DIN; ++a)
                   if (a < d_in) sw[a] = fmaf(g, xsbuf[r * TDG_MAX_DIN + a], sw[a]);
-              } else if (o == 1) {
-                const int ax = G.st_axis[sr];
+              } else {
 #pragma unroll
                 for (int a = 0; a < TDG_MAX_DIN; ++a)
                   if (a == ax) sw[a] += g;
@@ -929,8 +930,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         float* db0 = grad + A.b_off[0];
         for (int e = tid; e < N * (1 + d_in); e += NTC) {
           const int n = e % N, c = e / N;   // c = 0: bias, c = 1 + a: weight column a
-          const float v = red[128 * c + n] + red[640 + 128 * c + n] + red[1280 + 128 * c + n] +
-                          red[1920 + 128 * c + n];
+          float v = red[128 * c + n];
+#pragma unroll
+          for (int q = 1; q < NPART; ++q) v += red[640 * q + 128 * c + n];
           float* dst = c == 0 ? &db0[n] : &dW0[n * d_in + (c - 1)];
           *dst = first ? v : *dst + v;
         }
@@ -956,7 +958,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       // dW operand A = dL/dZ_l^T [128 (neurons, zero padded) x 128 rows] from P1, and the bias
       // gradient of Linear l-1 (sum of dL/dZ_l over value rows) from the same reads
       {
-        float* red = ybuf;   // [4][128] bias partials
+        float* red = ybuf;   // [NPART][128] bias partials
         const int n = tid & 127;
         float sb = 0.f;
         for (int e = tid; e < 128 * 32; e += NTC) {
@@ -977,7 +979,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         __syncthreads();
         float* db = grad + A.b_off[l - 1];
         for (int m = tid; m < N; m += NTC) {
-          const float v = red[m] + red[128 + m] + red[256 + m] + red[384 + m];
+          float v = red[m];
+#pragma unroll
+          for (int q = 1; q < NPART; ++q) v += red[128 * q + m];
           db[m] = first ? v : db[m] + v;
         }
       }
@@ -1028,7 +1032,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       // tile, so the accumulation order is fixed.
       {
         float4* stage = reinterpret_cast<float4*>(opA);
-        for (int c = 8 * cgrp; c < kp; c += 32) {
+        for (int c = 8 * cgrp; c < kp; c += 8 * NCG) {
           float v[8];
           tmem_ld8(D2 + lane_addr + c, v);
           const int j = c >> 2, sw = lrow & 7;
