@@ -1,6 +1,7 @@
 """Build libtdg.so (the C-ABI CUDA library) in-tree with nvcc for sm_103a.
 
-Each translation unit compiles in parallel; the shared library links against the CUDA runtime.
+Every object compiles in parallel (the tensor-core kernel once per precision and main site
+class, from tdg_tc_inst.cu); the shared library links against the CUDA runtime.
 Usage: python -m torch_de_solver_gb300.csrc.build  (or build() from Python).
 """
 import concurrent.futures
@@ -12,8 +13,18 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
-SOURCES = ['tdg_tc_3x.cu', 'tdg_tc_tf32.cu', 'tdg_tc_bf16.cu', 'tdg_plan.cu', 'tdg_fused.cu',
-           'tdg_fused_tc.cu', 'tdg_plain.cu', 'tdg_util.cu', 'tdg_noalloc.cu']
+SOURCES = ['tdg_plan.cu', 'tdg_fused.cu', 'tdg_fused_tc.cu', 'tdg_plain.cu', 'tdg_util.cu',
+           'tdg_noalloc.cu']
+# the tensor-core kernel: one object per (precision, main site class), from tdg_tc_inst.cu
+TC_PRECISIONS = (('tf32', 0, 0), ('bf16', 1, 0), ('3x', 0, 1))
+TC_CLASSES = 11   # jetcls::N_CLASSES in tdg_jetcls.h
+
+
+def units():
+    out = [(f'tdg_tc_inst.cu', f'tdg_tc_{p}_c{c}.o',
+            [f'-DTDG_TC_PREC={p}', f'-DTDG_TC_BF16={b}', f'-DTDG_TC_X3={x}', f'-DTDG_TC_CLS={c}'])
+           for p, b, x in TC_PRECISIONS for c in range(TC_CLASSES)]
+    return out + [(src, src.replace('.cu', '.o'), []) for src in SOURCES]
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 LIB = os.path.join(PKG, 'libtdg.so')
 
@@ -34,16 +45,18 @@ def build(verbose=False, extra=()):
         flags += ['-Xptxas', '-v']
     cc = nvcc()
 
-    def compile_one(src):
-        obj = os.path.join(obj_dir, src.replace('.cu', '.o'))
-        cmd = [cc, *flags, '-c', os.path.join(HERE, src), '-o', obj]
+    def compile_one(unit):
+        src, obj_name, defines = unit
+        obj = os.path.join(obj_dir, obj_name)
+        cmd = [cc, *flags, *defines, '-c', os.path.join(HERE, src), '-o', obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f'nvcc failed for {src}:\n{r.stdout}\n{r.stderr}')
+            raise RuntimeError(f'nvcc failed for {obj_name}:\n{r.stdout}\n{r.stderr}')
         return obj, r.stderr
 
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(compile_one, SOURCES))
+    jobs = units()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, os.cpu_count() or 1)) as ex:
+        results = list(ex.map(compile_one, jobs))
     if verbose:
         for _, log in results:
             sys.stderr.write(log)

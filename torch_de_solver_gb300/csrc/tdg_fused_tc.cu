@@ -26,10 +26,21 @@ cudaError_t launch_bounded_wait_selftest(int max_polls, int* gave_up, cudaStream
   return cudaGetLastError();
 }
 
+namespace {
+using TcFn = cudaError_t (*)(const FusedArgs&, const TcLaunch&, int, cudaStream_t);
+#define TDG_TC_ENTRY(P, C) TDG_TC_FN(P, C),
+const TcFn kTcTf32[] = {TDG_TC_EACH_CLASS(TDG_TC_ENTRY, tf32)};
+const TcFn kTcBf16[] = {TDG_TC_EACH_CLASS(TDG_TC_ENTRY, bf16)};
+const TcFn kTc3x[] = {TDG_TC_EACH_CLASS(TDG_TC_ENTRY, 3x)};
+#undef TDG_TC_ENTRY
+static_assert(sizeof(kTcTf32) / sizeof(kTcTf32[0]) == jetcls::N_CLASSES, "one variant per site class");
+}  // namespace
+
 cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
-  if (t.x3) return launch_tc_3x(a, t, n_ctas, s);
-  if (t.bf16) return launch_tc_bf16(a, t, n_ctas, s);
-  return launch_tc_tf32(a, t, n_ctas, s);
+  const int c = t.cls_main >= 0 && t.cls_main < jetcls::N_CLASSES ? t.cls_main : 0;
+  if (t.x3) return kTc3x[c](a, t, n_ctas, s);
+  if (t.bf16) return kTcBf16[c](a, t, n_ctas, s);
+  return kTcTf32[c](a, t, n_ctas, s);
 }
 
 }  // namespace tdg

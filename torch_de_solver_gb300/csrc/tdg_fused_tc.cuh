@@ -1,6 +1,6 @@
 // Tensor-core fused training-step kernel (sm_103a, tcgen05 + TMEM + bulk copies), as templates.
-// Each precision variant is instantiated in its own translation unit (tdg_tc_tf32.cu,
-// tdg_tc_bf16.cu, tdg_tc_3x.cu) so that the three compile in parallel.
+// Each (precision, main site class) variant is instantiated in its own object, compiled from
+// tdg_tc_inst.cu with the variant's -D flags, so that all of them compile in parallel.
 //
 // Same computation as fused_fp32_kernel (tdg_fused.cu): one persistent CTA per SM walks tiles of
 // 128 (stream, point) rows through the tanh-jet forward, the operator program and loss, and the
@@ -220,14 +220,22 @@ __device__ __forceinline__ void sfor_(F& f, std::integer_sequence<int, I...>) {
 template <int N, typename F>
 __device__ __forceinline__ void sfor(F&& f) { sfor_(f, std::make_integer_sequence<int, N>{}); }
 
-// run f(integral_constant<C>) for the site class `cls`; false when cls is not a compiled class
-template <typename F>
+// run f(integral_constant<C>) for the site class `cls` when it is one this kernel carries: the
+// value-only class 0 and the plan's main class CM (each kernel instantiation carries two, which
+// keeps its code small); false otherwise (the table-driven code runs)
+template <int CM, typename F>
 __device__ __forceinline__ bool with_class(int cls, F&& f) {
-  bool done = false;
-  sfor<jetcls::N_CLASSES>([&](auto cc) {
-    if (cls == decltype(cc)::value) { f(cc); done = true; }
-  });
-  return done;
+  if (cls == 0) {
+    f(std::integral_constant<int, 0>{});
+    return true;
+  }
+  if constexpr (CM > 0) {
+    if (cls == CM) {
+      f(std::integral_constant<int, CM>{});
+      return true;
+    }
+  }
+  return false;
 }
 
 // f(T) with the points per tile T a compile-time constant when the group is a single site of
@@ -371,12 +379,13 @@ __device__ __forceinline__ void site_values_tab(const DevGroup& G, int q, const 
 
 // thread (p, 4 neurons): H of every (stream, point) row from interleaved FP32 pre-activations zs
 // (kp per row) into FP32 rows of P (stride LDS); tanh once per (point, neuron)
+template <int CM>
 __device__ void jet_rows_from_op(const unsigned char* __restrict__ zs, float* __restrict__ P,
                                  const DevGroup& G, int kp) {
   const int T = G.T, n4s = kp >> 2;
   for (int q = 0; q < G.n_sites; ++q) {
     const int base = G.site_streams[q][0];
-    if (with_class(G.site_cls[q], [&](auto cc) {
+    if (with_class<CM>(G.site_cls[q], [&](auto cc) {
           with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
             const int Tc = tq;
             for (int e = threadIdx.x; e < Tc * n4s; e += NTC) {
@@ -423,7 +432,7 @@ __device__ void rows_to_opT(const float* __restrict__ P, unsigned char* __restri
 // highest order down, the value stream last, so every Z a rule reads is still intact).
 // When tsave is given, t = tanh(z) of every value row is also stored there (the saved
 // pre-activations of the layer, interleaved FP32), for the backward pass.
-template <bool BF16>
+template <bool BF16, int CM>
 __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ out,
                              const DevGroup& G, int np, bool inplace, bool also_out,
                              unsigned char* __restrict__ tsave) {
@@ -433,7 +442,7 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
     const int ns = G.site_nstreams[q];
     const int base = G.site_streams[q][0];
     // classed site: one loop per class, the dispatch outside it
-    if (with_class(G.site_cls[q], [&](auto cc) {
+    if (with_class<CM>(G.site_cls[q], [&](auto cc) {
           with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
             const int Tc = tq;
             for (int e = threadIdx.x; e < Tc * n4s; e += NTC)
@@ -514,7 +523,7 @@ struct TcArgs {
   int* err;                                   // set when a bounded wait gives up
 };
 
-template <bool BF16, bool X3>
+template <bool BF16, bool X3, int CM>
 __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA) {
   constexpr int ES = BF16 ? 2 : 4;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -646,14 +655,14 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     __syncthreads();
     unsigned char* t0 = A.do_grad ? reinterpret_cast<unsigned char*>(scr) : nullptr;
     if (L == 2) {
-      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true, false, t0);   // last hidden layer: rows in P1
+      jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), true, false, t0);   // last hidden layer: rows in P1
     } else if (X3) {
-      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), true, true, t0);
+      jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), true, true, t0);
       zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
       __syncthreads();
       alo_from_rows(P1, ALO, p16(A.width[1]), lane_addr, lrow, cgrp);
     } else {
-      jet_fwd_rows<BF16>(P1, opA, G, p16(A.width[1]), false, false, t0);
+      jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), false, false, t0);
       zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
     }
     cx.publish();
@@ -698,14 +707,14 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       __syncthreads();
       unsigned char* tj = A.do_grad ? reinterpret_cast<unsigned char*>(scr + (int64_t)j * scr_slot) : nullptr;
       if (j == L - 2) {
-        jet_fwd_rows<BF16>(P1, opA, G, np, true, false, tj);   // last hidden layer: FP32 rows in P1
+        jet_fwd_rows<BF16, CM>(P1, opA, G, np, true, false, tj);   // last hidden layer: FP32 rows in P1
       } else if (X3) {
-        jet_fwd_rows<BF16>(P1, opA, G, np, true, true, tj);
+        jet_fwd_rows<BF16, CM>(P1, opA, G, np, true, true, tj);
         zero_rows<BF16>(opA, R, np, ES);
         __syncthreads();
         alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
       } else {
-        jet_fwd_rows<BF16>(P1, opA, G, np, false, false, tj);
+        jet_fwd_rows<BF16, CM>(P1, opA, G, np, false, false, tj);
         zero_rows<BF16>(opA, R, np, ES);
       }
       cx.publish();
@@ -866,7 +875,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         for (int q = 0; q < G.n_sites; ++q) {
           const int ns = G.site_nstreams[q];
           const int base = G.site_streams[q][0];
-          if (with_class(G.site_cls[q], [&](auto cc) {
+          if (with_class<CM>(G.site_cls[q], [&](auto cc) {
                 with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
                   const int Tc = tq;
                   for (int e = tid; e < Tc * n4s; e += NTC)
@@ -989,7 +998,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       // H_{l-1}: the tanh jets of Z_{l-1} (opB) per (point, 4 neurons), every stream of a site
       // at once, as FP32 rows in P1 (dL/dZ_l there is consumed)
       cx.wait_tma();
-      jet_rows_from_op(opB, P1, G, kp);
+      jet_rows_from_op<CM>(opB, P1, G, kp);
       cx.publish();
       if (X3) {
         // split TF32: two halves of 64 rows, [hi | lo] of H_{l-1}^T for the half in opB, then
@@ -1098,12 +1107,12 @@ __global__ void pack_weights_kernel(const float* __restrict__ params, TcLaunch t
   }
 }
 
-template <bool BF16, bool X3>
+template <bool BF16, bool X3, int CM>
 cudaError_t launch_variant(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s) {
   static bool attr = false;
   const size_t smem = fused_tc_smem_bytes();
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(fused_tc_kernel<BF16, X3>,
+    cudaError_t e = cudaFuncSetAttribute(fused_tc_kernel<BF16, X3, CM>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr = true;
@@ -1116,7 +1125,7 @@ cudaError_t launch_variant(const FusedArgs& a, const TcLaunch& t, int n_ctas, cu
   ta.wpack = t.wpack;
   for (int l = 0; l < TDG_MAX_LAYERS; ++l) { ta.wfwd_off[l] = t.fwd_off[l]; ta.wbwd_off[l] = t.bwd_off[l]; }
   ta.err = t.err;
-  fused_tc_kernel<BF16, X3><<<n_ctas, NTC, smem, s>>>(a, ta);
+  fused_tc_kernel<BF16, X3, CM><<<n_ctas, NTC, smem, s>>>(a, ta);
   count_launch();
   return cudaGetLastError();
 }

@@ -110,6 +110,7 @@ cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s);
 struct TcLaunch {
   bool bf16;
   bool x3;     // split TF32 (hi*hi + hi*lo + lo*hi)
+  int cls_main;   // the site class (besides the value-only class 0) the kernel variant carries
   unsigned char* wpack;
   int64_t fwd_off[TDG_MAX_LAYERS], bwd_off[TDG_MAX_LAYERS];
   int64_t w_off[TDG_MAX_LAYERS];
@@ -151,9 +152,15 @@ struct PlainArgs {
 };
 cudaError_t run_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
-cudaError_t launch_tc_tf32(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
-cudaError_t launch_tc_bf16(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
-cudaError_t launch_tc_3x(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
+// the tensor-core kernel's variants: launch_tc_<precision>_c<main site class>
+#define TDG_TC_FN_(P, C) launch_tc_##P##_c##C
+#define TDG_TC_FN(P, C) TDG_TC_FN_(P, C)
+#define TDG_TC_DECLARE(P, C) \
+  cudaError_t TDG_TC_FN(P, C)(const FusedArgs& a, const TcLaunch& t, int n_ctas, cudaStream_t s);
+#define TDG_TC_EACH_CLASS(M, P) M(P, 0) M(P, 1) M(P, 2) M(P, 3) M(P, 4) M(P, 5) M(P, 6) M(P, 7) M(P, 8) M(P, 9) M(P, 10)
+TDG_TC_EACH_CLASS(TDG_TC_DECLARE, tf32)
+TDG_TC_EACH_CLASS(TDG_TC_DECLARE, bf16)
+TDG_TC_EACH_CLASS(TDG_TC_DECLARE, 3x)
 cudaError_t launch_bounded_wait_selftest(int max_polls, int* gave_up, cudaStream_t s);
 cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
                                const int32_t* seg_list, int n_problems, int64_t n_params,

@@ -57,6 +57,7 @@ struct tdg_plan {
   int64_t n_params = 0, part_stride = 0;
   int n_problems = 0, n_slots = 0, n_tiles = 0, n_ctas = 0, n_segments = 0, max_streams = 0;
   int precision = 0, form = 0;
+  int cls_main = 0;   // the tensor-core kernel variant: the site class with the most rows
   double flops_hidden = 0, flops_total = 0;
   std::vector<const float*> arrays;
   std::vector<int64_t> array_len;
@@ -436,6 +437,18 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     p->flops_hidden += 3.0 * 2.0 * (double)g.n_rows * S * hidden_pairs;
     p->flops_total += 3.0 * 2.0 * (double)g.n_rows * S * all_pairs;
   }
+  // the tensor-core kernel variant: besides the value-only class, it carries the compile-time
+  // jets of one site class, the one covering the most rows (other sites run the tables)
+  {
+    std::vector<int64_t> rows_of_class(jetcls::N_CLASSES, 0);
+    for (int gi = 0; gi < d.n_groups; ++gi)
+      for (int q = 0; q < groups[gi].n_sites; ++q) {
+        const int c = groups[gi].site_cls[q];
+        if (c > 0) rows_of_class[c] += (int64_t)d.groups[gi].n_rows * groups[gi].site_nstreams[q];
+      }
+    for (int c = 1; c < jetcls::N_CLASSES; ++c)
+      if (rows_of_class[c] > rows_of_class[p->cls_main]) p->cls_main = c;
+  }
   // contiguous equal-count partition of the tile list over one CTA per SM
   int sms = 0;
   ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
@@ -615,6 +628,7 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
     TcLaunch t{};
     t.bf16 = p->precision == TDG_PREC_BF16;
     t.x3 = p->precision == TDG_PREC_3XTF32;
+    t.cls_main = p->cls_main;
     t.wpack = p->d_wpack;
     for (int l = 0; l < TDG_MAX_LAYERS; ++l) {
       t.fwd_off[l] = p->wpack_fwd[l];
