@@ -377,6 +377,73 @@ __device__ __forceinline__ void site_values_tab(const DevGroup& G, int q, const 
   }
 }
 
+// the table-driven forward jet of site q (out of line: the compiled classes are the hot path)
+template <bool BF16>
+__device__ __noinline__ void jet_fwd_tab(float* __restrict__ P, unsigned char* __restrict__ out,
+                                         const DevGroup& G, int q, int np, bool inplace, bool also_out,
+                                         unsigned char* __restrict__ tsave) {
+  const int T = G.T, n4s = np >> 2;
+  const int ns = G.site_nstreams[q], base = G.site_streams[q][0];
+  for (int e = threadIdx.x; e < T * n4s; e += NTC) {
+    const int p = e % T, n = (e / T) * 4;
+    Sig sg;
+    sg.make(ld4(&P[(base * T + p) * LDS + n]), false);
+    if (tsave) *reinterpret_cast<float4*>(tsave + ofs(base * T + p, n, np, 4)) = sg.t;
+    for (int m = ns - 1; m >= 0; --m) {
+      const int s = G.site_streams[q][m];
+      float4 h = sg.t;
+      if (m > 0) {
+        h = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < G.st_nrule[s]; ++u) {
+          const DevRule& ru = G.rules[s][u];
+          float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
+          for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4(&P[(ru.sub[f] * T + p) * LDS + n]));
+          h = f4add(h, v);
+        }
+      }
+      if (inplace) st4(&P[(s * T + p) * LDS + n], h);
+      if (!inplace || also_out) put4<BF16>(out, s * T + p, n, np, h);
+    }
+  }
+}
+
+// the table-driven jet adjoint of site q (out of line)
+template <bool BF16>
+__device__ __noinline__ void jet_bwd_tab(float* __restrict__ P1, const unsigned char* __restrict__ zs,
+                                         unsigned char* __restrict__ opA, const DevGroup& G, int q, int np,
+                                         bool write_op) {
+  const int T = G.T, n4s = np >> 2;
+  const int ns = G.site_nstreams[q], base = G.site_streams[q][0];
+  for (int e = threadIdx.x; e < T * n4s; e += NTC) {
+    const int p = e % T, n = (e / T) * 4;
+    Sig sg;
+    sg.from_t(ld4o(zs, ofs(base * T + p, n, np, 4)), true);   // the value row holds t
+    for (int m = 0; m < ns; ++m) {
+      const int b = G.site_streams[q][m];
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      const int pf = G.st_pull_first[b];
+      for (int u = 0; u < G.st_npull[b]; ++u) {
+        const DevPull& pl = G.pulls[pf + u];
+        float4 v = f4mul(ld4(&P1[(pl.alpha * T + p) * LDS + n]), f4scale(sg.sel(pl.kk), (float)pl.mult));
+        for (int f = 0; f < pl.n_oth; ++f) v = f4mul(v, ld4o(zs, ofs(pl.oth[f] * T + p, n, np, 4)));
+        acc = f4add(acc, v);
+      }
+      st4(&P1[(b * T + p) * LDS + n], acc);
+      if (write_op) put4<BF16>(opA, b * T + p, n, np, acc);
+    }
+  }
+}
+
+// the table-driven H rows of site q from interleaved pre-activations (out of line)
+__device__ __noinline__ void rows_from_op_tab(const unsigned char* __restrict__ zs, float* __restrict__ P,
+                                              const DevGroup& G, int q, int kp) {
+  const int T = G.T, n4s = kp >> 2, base = G.site_streams[q][0];
+  for (int e = threadIdx.x; e < T * n4s; e += NTC) {
+    const int p = e % T, n = (e / T) * 4;
+    site_values_tab(G, q, zs, kp, p, n, [&](int m, float4 h) { st4(&P[((base + m) * T + p) * LDS + n], h); });
+  }
+}
+
 // thread (p, 4 neurons): H of every (stream, point) row from interleaved FP32 pre-activations zs
 // (kp per row) into FP32 rows of P (stride LDS); tanh once per (point, neuron)
 template <int CM>
@@ -397,11 +464,7 @@ __device__ void jet_rows_from_op(const unsigned char* __restrict__ zs, float* __
           });
         }))
       continue;
-    for (int e = threadIdx.x; e < T * n4s; e += NTC) {
-      const int p = e % T, n = (e / T) * 4;
-      site_values_tab(G, q, zs, kp, p, n,
-                      [&](int m, float4 h) { st4(&P[((base + m) * T + p) * LDS + n], h); });
-    }
+    rows_from_op_tab(zs, P, G, q, kp);
   }
 }
 
@@ -451,27 +514,7 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
           });
         }))
       continue;
-    for (int e = threadIdx.x; e < T * n4s; e += NTC) {
-      const int p = e % T, n = (e / T) * 4;
-      Sig sg;
-      sg.make(ld4(&P[(base * T + p) * LDS + n]), false);
-      if (tsave) *reinterpret_cast<float4*>(tsave + ofs(base * T + p, n, np, 4)) = sg.t;
-      for (int m = ns - 1; m >= 0; --m) {
-        const int s = G.site_streams[q][m];
-        float4 h = sg.t;
-        if (m > 0) {
-          h = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int u = 0; u < G.st_nrule[s]; ++u) {
-            const DevRule& ru = G.rules[s][u];
-            float4 v = f4scale(sg.sel(ru.k), (float)ru.mult);
-            for (int f = 0; f < ru.k; ++f) v = f4mul(v, ld4(&P[(ru.sub[f] * T + p) * LDS + n]));
-            h = f4add(h, v);
-          }
-        }
-        if (inplace) st4(&P[(s * T + p) * LDS + n], h);
-        if (!inplace || also_out) put4<BF16>(out, s * T + p, n, np, h);
-      }
-    }
+    jet_fwd_tab<BF16>(P, out, G, q, np, inplace, also_out, tsave);
   }
 }
 
@@ -884,26 +927,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
                 });
               }))
             continue;
-          for (int e = tid; e < T * n4s; e += NTC) {
-            const int p = e % T, n = (e / T) * 4;
-            Sig sg;
-            sg.from_t(ld4o(opB, ofs(base * T + p, n, np, 4)), true);   // the value row holds t
-            for (int m = 0; m < ns; ++m) {
-              const int b = G.site_streams[q][m];
-              float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-              const int pf = G.st_pull_first[b];
-              for (int u = 0; u < G.st_npull[b]; ++u) {
-                const DevPull& pl = G.pulls[pf + u];
-                float4 v = f4mul(ld4(&P1[(pl.alpha * T + p) * LDS + n]),
-                                 f4scale(sg.sel(pl.kk), (float)pl.mult));
-                for (int f = 0; f < pl.n_oth; ++f) v = f4mul(v, ld4o(opB, ofs(pl.oth[f] * T + p, n, np, 4)));
-                acc = f4add(acc, v);
-              }
-              const float4 gz = acc;
-              st4(&P1[(b * T + p) * LDS + n], gz);
-              if (l >= 2) put4<BF16>(opA, b * T + p, n, np, gz);
-            }
-          }
+          jet_bwd_tab<BF16>(P1, opB, opA, G, q, np, l >= 2);
         }
       }
       if (l == 1) {
