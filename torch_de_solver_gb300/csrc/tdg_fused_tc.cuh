@@ -225,26 +225,28 @@ __device__ __forceinline__ void sfor(F&& f) { sfor_(f, std::make_integer_sequenc
 // keeps its code small); false otherwise (the table-driven code runs)
 template <int CM, typename F>
 __device__ __forceinline__ bool with_class(int cls, F&& f) {
-  if (cls == 0) {
-    f(std::integral_constant<int, 0>{});
-    return true;
-  }
+  if (cls == 0) return f(std::integral_constant<int, 0>{});
   if constexpr (CM > 0) {
-    if (cls == CM) {
-      f(std::integral_constant<int, CM>{});
-      return true;
-    }
+    if (cls == CM) return f(std::integral_constant<int, CM>{});
   }
   return false;
 }
 
 // f(T) with the points per tile T a compile-time constant when the group is a single site of
-// class C (then T = 128 / streams), else the group's runtime T
+// class C (then T = 128 / streams); for the value-only class also f(runtime T) for other groups.
+// False when neither applies (the table-driven code runs).
 template <int C, typename F>
-__device__ __forceinline__ void with_tile_points(const DevGroup& G, F&& f) {
+__device__ __forceinline__ bool with_tile_points(const DevGroup& G, F&& f) {
   constexpr int TC = RMAX / rules_of<C>().ns;
-  if (G.n_sites == 1 && G.T == TC) f(std::integral_constant<int, TC>{});
-  else f(G.T);
+  if (G.n_sites == 1 && G.T == TC) {
+    f(std::integral_constant<int, TC>{});
+    return true;
+  }
+  if constexpr (C == 0) {
+    f(G.T);
+    return true;
+  }
+  return false;
 }
 
 // H_M = sum_u mult * tanh^(k)(z_0) * prod Z[sub]  (same operation order as the table rules)
@@ -453,7 +455,7 @@ __device__ void jet_rows_from_op(const unsigned char* __restrict__ zs, float* __
   for (int q = 0; q < G.n_sites; ++q) {
     const int base = G.site_streams[q][0];
     if (with_class<CM>(G.site_cls[q], [&](auto cc) {
-          with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
+          return with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
             const int Tc = tq;
             for (int e = threadIdx.x; e < Tc * n4s; e += NTC) {
               const int p = e % Tc, n = (e / Tc) * 4;
@@ -506,7 +508,7 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
     const int base = G.site_streams[q][0];
     // classed site: one loop per class, the dispatch outside it
     if (with_class<CM>(G.site_cls[q], [&](auto cc) {
-          with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
+          return with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
             const int Tc = tq;
             for (int e = threadIdx.x; e < Tc * n4s; e += NTC)
               jet_fwd_cls<decltype(cc)::value, BF16>(P, out, Tc, base, e % Tc, (e / Tc) * 4, np, inplace,
@@ -919,7 +921,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           const int ns = G.site_nstreams[q];
           const int base = G.site_streams[q][0];
           if (with_class<CM>(G.site_cls[q], [&](auto cc) {
-                with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
+                return with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
                   const int Tc = tq;
                   for (int e = tid; e < Tc * n4s; e += NTC)
                     jet_bwd_cls<decltype(cc)::value, BF16>(P1, opB, opA, Tc, base, e % Tc, (e / Tc) * 4, np,
