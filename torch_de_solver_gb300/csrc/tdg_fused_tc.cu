@@ -6,7 +6,7 @@ namespace tdg {
 
 size_t fused_tc_smem_bytes() {
   return 2 * (size_t)OPB + sizeof(float) * (RMAX * LDS + 2 * RMAX * MAX_OUT + RMAX * TDG_MAX_DIN + PBUF) +
-         sizeof(DevGroup) + sizeof(double) * (MAX_OUT + (NTC / 32) * MAX_OUT) + 2 * sizeof(uint64_t) + 16 + 3 * 128;
+         sizeof(DevGroup) + sizeof(double) * (MAX_OUT + (NTC / 32) * MAX_OUT) + 3 * sizeof(uint64_t) + 16 + 3 * 128;
 }
 
 // Self-test of the bounded wait: one thread waits on an mbarrier that nothing arrives at and

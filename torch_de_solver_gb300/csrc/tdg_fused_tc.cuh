@@ -112,21 +112,47 @@ __device__ __forceinline__ void put4(unsigned char* buf, int i, int k, int kp, f
   }
 }
 
+// bulk copies go through two slots, each an mbarrier with its own phase: slot B (the B operand
+// buffer opB; issue / load / ensure / wait_tma) and slot A (the other buffer opA, which holds B
+// operands too when the A operands live in tensor memory; issue_a / ensure_a / wait_a)
 struct TcCtx {
   uint64_t* bar_mma;
   uint64_t* bar_tma;
-  uint32_t ph_mma, ph_tma;
+  uint64_t* bar_tma_a;
+  uint32_t ph_mma, ph_tma, ph_tma_a;
   int* err;
   __device__ __forceinline__ void wait_mma() {
     if (!mbar_wait(bar_mma, ph_mma) && threadIdx.x == 0) atomicExch(err, 1);
     ph_mma ^= 1;
     fence_after();
   }
-  bool inflight;   // a bulk copy issued and not yet waited for
+  bool inflight;     // slot B: a bulk copy issued and not yet waited for
+  bool inflight_a;   // slot A
   __device__ __forceinline__ void wait_tma() {
     if (!mbar_wait(bar_tma, ph_tma) && threadIdx.x == 0) atomicExch(err, 2);
     ph_tma ^= 1;
     inflight = false;
+  }
+  __device__ __forceinline__ void wait_a() {
+    if (!mbar_wait(bar_tma_a, ph_tma_a) && threadIdx.x == 0) atomicExch(err, 3);
+    ph_tma_a ^= 1;
+    inflight_a = false;
+  }
+  __device__ __forceinline__ void issue_a(void* dst, const void* src, uint32_t bytes) {
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(bar_tma_a, bytes);
+      bulk_g2s(dst, src, bytes, bar_tma_a);
+    }
+    inflight_a = true;
+  }
+  __device__ __forceinline__ void ensure_a(void* dst, const void* src, uint32_t bytes) {
+    if (!inflight_a) issue_a(dst, src, bytes);
+    wait_a();
+  }
+  // no copy left in flight (before the CTA exits)
+  __device__ __forceinline__ void drain() {
+    if (inflight) wait_tma();
+    if (inflight_a) wait_a();
   }
   // every thread: generic-proxy shared-memory accesses ordered before the async proxy's (MMA
   // operand reads, bulk copies into shared memory), then barrier
@@ -534,6 +560,81 @@ __device__ void alo_from_rows(const float* __restrict__ P, uint32_t a_lo, int kp
   tmem_st_wait();
 }
 
+// A operand rows into tensor memory (lane = row, column = K): hi = tf32(x) at a_hi and, for split
+// TF32, lo = x - hi at a_lo; rows >= R are zero. Each warp writes its own lane quarter.
+template <bool X3>
+__device__ void rows_to_tmem(const float* __restrict__ P, uint32_t a_hi, uint32_t a_lo, int kp, int R,
+                             uint32_t lane_addr, int lrow, int cgrp) {
+  for (int c = 8 * cgrp; c < kp; c += 8 * NCG) {
+    float x[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (lrow < R) {
+      const float4 x0 = ld4(&P[lrow * LDS + c]), x1 = ld4(&P[lrow * LDS + c + 4]);
+      x[0] = x0.x; x[1] = x0.y; x[2] = x0.z; x[3] = x0.w;
+      x[4] = x1.x; x[5] = x1.y; x[6] = x1.z; x[7] = x1.w;
+    }
+    float hi[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) hi[i] = to_tf32(x[i]);
+    tmem_st8(a_hi + lane_addr + c, hi);
+    if (X3) {
+      float lo[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) lo[i] = x[i] - hi[i];
+      tmem_st8(a_lo + lane_addr + c, lo);
+    }
+  }
+  tmem_st_wait();
+}
+
+// D[128 x n] = A . B^T with A (rows x k) in tensor memory (hi at a_hi, split TF32 lo at a_lo) and
+// the packed B from global memory: split TF32 streams K-half 0 ([hi | lo]) through slot A into
+// bufA and K-half 1 through slot B into bufB, and issues K-half 0's MMAs while K-half 1 lands;
+// TF32 takes all of B through slot A. Copies issued ahead are waited for, not reissued.
+template <bool X3>
+__device__ void gemm_tmem_a(TcCtx& cx, uint32_t d, uint32_t a_hi, uint32_t a_lo, unsigned char* bufA,
+                            unsigned char* bufB, const unsigned char* b_src, int n, int k) {
+  const uint32_t idesc = instr_desc<false>(128, n);
+  if (X3) {
+    const int kh = k / 2;
+    const uint32_t hb = (uint32_t)n * kh * 4;   // one of [hi | lo] of a K-half
+    const uint32_t sbo = (uint32_t)(kh / 4) * 128;
+    cx.ensure_a(bufA, b_src, 2 * hb);
+    if (threadIdx.x == 0) {
+      fence_after();
+      const uint32_t b0 = smem_u32(bufA);
+      for (int j = 0; j < kh / 8; ++j) {
+        const uint64_t bh = smem_desc(b0 + j * 256, 128, sbo), bl = smem_desc(b0 + hb + j * 256, 128, sbo);
+        mma_ts_tf32(d, a_hi + 8 * j, bh, idesc, j > 0);
+        mma_ts_tf32(d, a_hi + 8 * j, bl, idesc, true);
+        mma_ts_tf32(d, a_lo + 8 * j, bh, idesc, true);
+      }
+    }
+    cx.ensure(bufB, b_src + 2 * hb, 2 * hb);
+    if (threadIdx.x == 0) {
+      fence_after();
+      const uint32_t b0 = smem_u32(bufB);
+      for (int j = 0; j < kh / 8; ++j) {
+        const int kk = kh + 8 * j;
+        const uint64_t bh = smem_desc(b0 + j * 256, 128, sbo), bl = smem_desc(b0 + hb + j * 256, 128, sbo);
+        mma_ts_tf32(d, a_hi + kk, bh, idesc, true);
+        mma_ts_tf32(d, a_hi + kk, bl, idesc, true);
+        mma_ts_tf32(d, a_lo + kk, bh, idesc, true);
+      }
+      commit(cx.bar_mma);
+    }
+  } else {
+    cx.ensure_a(bufA, b_src, (uint32_t)n * k * 4);
+    if (threadIdx.x == 0) {
+      fence_after();
+      const uint32_t b0 = smem_u32(bufA), sbo = (uint32_t)(k / 4) * 128;
+      for (int j = 0; j < k / 8; ++j)
+        mma_ts_tf32(d, a_hi + 8 * j, smem_desc(b0 + j * 256, 128, sbo), idesc, j > 0);
+      commit(cx.bar_mma);
+    }
+  }
+  cx.wait_mma();
+}
+
 // dL/dH rows from the dX accumulator (tensor memory) into plain FP32 rows, zero past K and R
 __device__ __forceinline__ void d1_to_rows(uint32_t d1, float* __restrict__ P, int kp, int K, int R,
                                            uint32_t lane_addr, int lrow, int cgrp) {
@@ -571,6 +672,9 @@ struct TcArgs {
 template <bool BF16, bool X3, int CM>
 __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA) {
   constexpr int ES = BF16 ? 2 : 4;
+  // TF32 and split TF32 keep every A operand in tensor memory (hi at AHI, lo at ALO), which
+  // leaves both shared-memory operand buffers to the B operands; BF16 keeps A in opA
+  constexpr bool TMA_A = !BF16;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* opA = smem_raw;
   unsigned char* opB = smem_raw + OPB;
@@ -583,7 +687,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   double* cur_slot = reinterpret_cast<double*>(Gs + 1);        // [MAX_OUT]
   double* wred = cur_slot + MAX_OUT;                           // [NTC/32][MAX_OUT]
   uint64_t* bars = reinterpret_cast<uint64_t*>(wred + (NTC / 32) * MAX_OUT);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3);
   int8_t* row_s = reinterpret_cast<int8_t*>(tmem_slot + 4);     // [128] stream of a row, -1 padding
   uint8_t* row_v = reinterpret_cast<uint8_t*>(row_s + 128);     // [128] 1 on value-stream rows
   int8_t* row_ax = reinterpret_cast<int8_t*>(row_v + 128);      // [128] -1 value row, axis of a first
@@ -599,17 +703,19 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   if (tid == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) tmem_alloc(tmem_slot, X3 ? 512 : 256);
+  if (warp == 0) tmem_alloc(tmem_slot, TMA_A ? 512 : 256);
   for (int s = tid; s < A.n_slots; s += NTC) A.slot_partial[(int64_t)cta * A.n_slots + s] = 0.0;
   if (tid < MAX_OUT) cur_slot[tid] = 0.0;
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t D1 = *tmem_slot, D2 = *tmem_slot + 128;
-  const uint32_t ALO = *tmem_slot + 256;   // split TF32: low part of the A operand
-  TcCtx cx{&bars[0], &bars[1], 0u, 0u, TA.err, false};
+  const uint32_t AHI = *tmem_slot + 256;                    // the A operand (TF32 hi) in TMEM
+  const uint32_t ALO = *tmem_slot + (TMA_A ? 384 : 256);    // split TF32: its low part
+  TcCtx cx{&bars[0], &bars[1], &bars[2], 0u, 0u, 0u, TA.err, false, false};
   // TMEM lane quarter and column group of this warp in the epilogues
   const int lrow = 32 * (warp & 3) + lane;
   const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
@@ -618,7 +724,17 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   // the first bulk copy of hidden GEMM j's forward weights (split TF32: the first [hi | lo] half)
   auto wfwd_first = [&](int j) {
     const uint32_t nk = (uint32_t)p16(A.width[j + 1]) * p16(A.width[j]);
-    cx.issue(opB, TA.wpack + TA.wfwd_off[j], X3 ? nk * 4 : nk * ES);
+    if constexpr (TMA_A) {   // split TF32: K-half 0 -> opA, K-half 1 -> opB; TF32: all -> opA
+      cx.issue_a(opA, TA.wpack + TA.wfwd_off[j], nk * 4);
+      if (X3) cx.issue(opB, TA.wpack + TA.wfwd_off[j] + nk * 4, nk * 4);
+    } else {
+      cx.issue(opB, TA.wpack + TA.wfwd_off[j], X3 ? nk * 4 : nk * ES);
+    }
+  };
+  // the first bulk copy of the dX GEMM's B operand (W^T of Linear j): slot A into opA
+  auto wbwd_first = [&](int j) {
+    const uint32_t nk = (uint32_t)p16(A.width[j + 1]) * p16(A.width[j]);
+    cx.issue_a(opA, TA.wpack + TA.wbwd_off[j], nk * 4);
   };
 
   for (int ti = A.cta_tile_begin[cta]; ti < A.cta_tile_begin[cta + 1]; ++ti) {
@@ -701,6 +817,10 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     unsigned char* t0 = A.do_grad ? reinterpret_cast<unsigned char*>(scr) : nullptr;
     if (L == 2) {
       jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), true, false, t0);   // last hidden layer: rows in P1
+    } else if constexpr (TMA_A) {   // H rows in P1, then hi (and lo) into tensor memory
+      jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), true, false, t0);
+      __syncthreads();
+      rows_to_tmem<X3>(P1, AHI, ALO, p16(A.width[1]), R, lane_addr, lrow, cgrp);
     } else if (X3) {
       jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), true, true, t0);
       zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
@@ -716,14 +836,17 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     for (int j = 1; j < L - 1; ++j) {
       const int K = A.width[j], N = A.width[j + 1];
       const int kp = p16(K), np = p16(N);
-      if (X3) {
+      if constexpr (TMA_A) {
+        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, TA.wpack + TA.wfwd_off[j], np, kp);
+      } else if (X3) {
         gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wfwd_off[j], np, kp);
       } else {
         cx.ensure(opB, TA.wpack + TA.wfwd_off[j], (uint32_t)(np * kp * ES));
         gemm_issue<BF16>(D1, opA, opB, np, kp, cx.bar_mma);
         cx.wait_mma();
       }
-      if (j + 1 < L - 1) wfwd_first(j + 1);   // opB is free: overlaps the epilogue and the jets
+      if (j + 1 < L - 1) wfwd_first(j + 1);   // the buffers are free: overlaps the epilogue and the jets
+      else if (TMA_A && A.do_grad) wbwd_first(L - 2);   // the first dX GEMM's W^T, during the program
       // epilogue: D1 -> +bias -> P1 (plain) and scratch slot j (interleaved FP32)
       {
         const float* bj = pbuf + PB_HB + (j - 1) * TDG_MAX_WIDTH;
@@ -753,6 +876,10 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       unsigned char* tj = A.do_grad ? reinterpret_cast<unsigned char*>(scr + (int64_t)j * scr_slot) : nullptr;
       if (j == L - 2) {
         jet_fwd_rows<BF16, CM>(P1, opA, G, np, true, false, tj);   // last hidden layer: FP32 rows in P1
+      } else if constexpr (TMA_A) {
+        jet_fwd_rows<BF16, CM>(P1, opA, G, np, true, false, tj);
+        __syncthreads();
+        rows_to_tmem<X3>(P1, AHI, ALO, np, R, lane_addr, lrow, cgrp);
       } else if (X3) {
         jet_fwd_rows<BF16, CM>(P1, opA, G, np, true, true, tj);
         zero_rows<BF16>(opA, R, np, ES);
@@ -925,11 +1052,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
                   const int Tc = tq;
                   for (int e = tid; e < Tc * n4s; e += NTC)
                     jet_bwd_cls<decltype(cc)::value, BF16>(P1, opB, opA, Tc, base, e % Tc, (e / Tc) * 4, np,
-                                                           l >= 2);
+                                                           !TMA_A && l >= 2);
                 });
               }))
             continue;
-          jet_bwd_tab<BF16>(P1, opB, opA, G, q, np, l >= 2);
+          jet_bwd_tab<BF16>(P1, opB, opA, G, q, np, !TMA_A && l >= 2);
         }
       }
       if (l == 1) {
@@ -974,14 +1101,24 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         break;
       }
       const int K = A.width[l - 1], kp = p16(K);
-      zero_rows<BF16>(opA, R, np, ES);
-      if (X3) {
+      if constexpr (TMA_A) {
         __syncthreads();
-        alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
+        rows_to_tmem<X3>(P1, AHI, ALO, np, R, lane_addr, lrow, cgrp);   // dL/dZ_l: the dX A operand
+        cx.publish();
+        if (X3)   // opB (Z_l) is free: K-half 1 of W_{l-1}^T lands while K-half 0's MMAs run
+          cx.issue(opB, TA.wpack + TA.wbwd_off[l - 1] + (uint32_t)kp * np * 4, (uint32_t)kp * np * 4);
+      } else {
+        zero_rows<BF16>(opA, R, np, ES);
+        if (X3) {
+          __syncthreads();
+          alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
+        }
+        cx.publish();
       }
-      cx.publish();
       // dX: D1[rows x kp] = dL/dZ_l[rows x np] . (W_{l-1}^T packed [kp x np])^T
-      if (X3) {
+      if constexpr (TMA_A) {
+        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, TA.wpack + TA.wbwd_off[l - 1], kp, np);
+      } else if (X3) {
         gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wbwd_off[l - 1], kp, np);
       } else {
         cx.load(opB, TA.wpack + TA.wbwd_off[l - 1], (uint32_t)(kp * np * ES));
@@ -1004,12 +1141,18 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             v[i] = (n < N && r + i < R) ? P1[(r + i) * LDS + n] : 0.f;
             if (row_v[r + i]) sb += v[i];
           }
-          put4<BF16>(opA, n, r, 128, make_float4(v[0], v[1], v[2], v[3]));
-          if (X3)   // lane = neuron n, columns = rows r..r+3 (the same r for the whole warp)
-            tmem_st4(ALO + lane_addr + r, v[0] - to_tf32(v[0]), v[1] - to_tf32(v[1]),
-                     v[2] - to_tf32(v[2]), v[3] - to_tf32(v[3]));
+          if constexpr (TMA_A) {   // lane = neuron n, columns = rows r..r+3 (the same r for the warp)
+            const float h0 = to_tf32(v[0]), h1 = to_tf32(v[1]), h2 = to_tf32(v[2]), h3 = to_tf32(v[3]);
+            tmem_st4(AHI + lane_addr + r, h0, h1, h2, h3);
+            if (X3) tmem_st4(ALO + lane_addr + r, v[0] - h0, v[1] - h1, v[2] - h2, v[3] - h3);
+          } else {
+            put4<BF16>(opA, n, r, 128, make_float4(v[0], v[1], v[2], v[3]));
+            if (X3)   // lane = neuron n, columns = rows r..r+3 (the same r for the whole warp)
+              tmem_st4(ALO + lane_addr + r, v[0] - to_tf32(v[0]), v[1] - to_tf32(v[1]),
+                       v[2] - to_tf32(v[2]), v[3] - to_tf32(v[3]));
+          }
         }
-        if (X3) tmem_st_wait();
+        if (TMA_A || X3) tmem_st_wait();
         red[(tid >> 7) * 128 + n] = sb;
         __syncthreads();
         float* db = grad + A.b_off[l - 1];
@@ -1026,7 +1169,43 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       cx.wait_tma();
       jet_rows_from_op<CM>(opB, P1, G, kp);
       cx.publish();
-      if (X3) {
+      if constexpr (TMA_A) {
+        // H_{l-1}^T as the B operand (K = rows): split TF32 puts rows 0..63 ([hi | lo]) in opA and
+        // rows 64..127 in opB, TF32 all rows in opA; A = dL/dZ_l^T (hi, lo) in tensor memory
+        const uint32_t idesc = instr_desc<false>(128, kp);
+        if (X3) {
+          const uint32_t lo_off = (uint32_t)kp * 64 * 4;
+          rows_to_opT<false, true>(P1, opA, kp, 0, 64, R, lo_off);
+          rows_to_opT<false, true>(P1, opB, kp, 64, 64, R, lo_off);
+          cx.publish();
+          if (tid == 0) {
+            for (int hh = 0; hh < 2; ++hh) {
+              const uint32_t b0 = smem_u32(hh ? opB : opA);
+              for (int j = 0; j < 8; ++j) {
+                const int kk = 64 * hh + 8 * j;
+                const uint64_t bh = smem_desc(b0 + j * 256, 128, 2048);
+                const uint64_t bl = smem_desc(b0 + lo_off + j * 256, 128, 2048);
+                mma_ts_tf32(D2, AHI + kk, bh, idesc, hh > 0 || j > 0);
+                mma_ts_tf32(D2, AHI + kk, bl, idesc, true);
+                mma_ts_tf32(D2, ALO + kk, bh, idesc, true);
+              }
+            }
+            commit(cx.bar_mma);
+          }
+        } else {
+          rows_to_opT<false, false>(P1, opA, kp, 0, 128, R, 0);
+          cx.publish();
+          if (tid == 0) {
+            const uint32_t b0 = smem_u32(opA);
+            for (int j = 0; j < 16; ++j)
+              mma_ts_tf32(D2, AHI + 8 * j, smem_desc(b0 + j * 256, 128, 4096), idesc, j > 0);
+            commit(cx.bar_mma);
+          }
+        }
+        cx.wait_mma();
+        cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
+        d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);
+      } else if (X3) {
         // split TF32: two halves of 64 rows, [hi | lo] of H_{l-1}^T for the half in opB, then
         // hi*hi + hi*lo + lo*hi per K-step (A lo = dL/dZ_l^T low part in tensor memory)
         const uint32_t lo_off = (uint32_t)kp * 64 * 4;
@@ -1082,8 +1261,13 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             red_add4(&dW[(int64_t)n * K + 4 * lane], v.x, v.y, v.z, v.w);
           }
       }
-      fence_before();
-      __syncthreads();
+      if constexpr (TMA_A) {
+        cx.publish();                         // the flush's reads of opA before the copy below
+        if (l - 1 >= 2) wbwd_first(l - 2);    // the next dX GEMM's W^T (K-half 0), during its jets
+      } else {
+        fence_before();
+        __syncthreads();
+      }
     }
   }
   __syncthreads();
@@ -1091,7 +1275,8 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     A.slot_partial[(int64_t)cta * A.n_slots + Gs->slot_first + tid] += cur_slot[tid];
   fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(*tmem_slot, X3 ? 512 : 256);
+  cx.drain();
+  if (warp == 0) tmem_dealloc(*tmem_slot, TMA_A ? 512 : 256);
 }
 
 // ---- weight packing: every hidden Linear j into forward (N x K) and transposed (K x N) operands.
