@@ -791,26 +791,54 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const int N = A.width[1], np = p16(N);
       const float* W0 = pbuf + PB_W0;
       const float* b0 = pbuf + PB_B0;
-      for (int e = tid; e < RMAX * (np >> 2); e += NTC) {
-        const int r = e % RMAX, n = (e / RMAX) * 4;
-        const int ax = row_ax[r];   // a value row: W0 x + b0; d/dx_a: column a of W0; else 0
-        float z[4] = {0.f, 0.f, 0.f, 0.f};
+      // a thread keeps one row in every iteration (NTC is a multiple of RMAX): its kind and
+      // coordinates load once; W0 and b0 of 4 neurons are 16-byte vectors (widths are multiples
+      // of 4); the input width is a compile-time constant of each branch
+      static_assert(NTC % RMAX == 0, "a thread keeps its row");
+      const int r = tid % RMAX;
+      const int ax = row_ax[r];   // a value row: W0 x + b0; d/dx_a: column a of W0; else 0
+      unsigned char* s0 = reinterpret_cast<unsigned char*>(scr);
+      auto layer = [&](auto din) {
+        constexpr int D = decltype(din)::value;
+        float x[D];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int nn = n + i;
-          if (nn >= N) continue;
-          if (ax == -1) {
-            float v = 0.f;
-            for (int a = 0; a < d_in; ++a) v = fmaf(W0[nn * d_in + a], xsbuf[r * TDG_MAX_DIN + a], v);
-            z[i] = v + b0[nn];
-          } else if (ax >= 0) {
-            z[i] = W0[nn * d_in + ax];
+        for (int a = 0; a < D; ++a) x[a] = xsbuf[r * TDG_MAX_DIN + a];
+        for (int e = tid; e < RMAX * (np >> 2); e += NTC) {
+          const int n = (e / RMAX) * 4;
+          float z[4] = {0.f, 0.f, 0.f, 0.f};
+          if (n < N) {
+            if (ax == -1) {
+              float w[4 * D];
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                const float4 wv = ld4(&W0[n * D + 4 * c]);
+                w[4 * c] = wv.x; w[4 * c + 1] = wv.y; w[4 * c + 2] = wv.z; w[4 * c + 3] = wv.w;
+              }
+              const float4 bv = ld4(&b0[n]);
+              const float bb[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+              for (int i = 0; i < 4; ++i) {
+                float v = 0.f;
+#pragma unroll
+                for (int a = 0; a < D; ++a) v = fmaf(w[i * D + a], x[a], v);
+                z[i] = v + bb[i];
+              }
+            } else if (ax >= 0) {
+#pragma unroll
+              for (int i = 0; i < 4; ++i) z[i] = W0[(n + i) * D + ax];
+            }
           }
+          const float4 zv = make_float4(z[0], z[1], z[2], z[3]);
+          st4(&P1[r * LDS + n], zv);
+          if (A.do_grad && ax != -1)   // value rows: the jets save t = tanh(z) instead
+            *reinterpret_cast<float4*>(s0 + ofs(r, n, np, 4)) = zv;
         }
-        const float4 zv = make_float4(z[0], z[1], z[2], z[3]);
-        st4(&P1[r * LDS + n], zv);
-        if (A.do_grad && ax != -1)   // value rows: the jets save t = tanh(z) instead
-          *reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(scr) + ofs(r, n, np, 4)) = zv;
+      };
+      switch (d_in) {
+        case 1: layer(std::integral_constant<int, 1>{}); break;
+        case 2: layer(std::integral_constant<int, 2>{}); break;
+        case 3: layer(std::integral_constant<int, 3>{}); break;
+        default: layer(std::integral_constant<int, 4>{}); break;
       }
     }
     __syncthreads();
@@ -1006,30 +1034,40 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const float* Wl = pbuf + PB_WL;
       float* dW = grad + A.w_off[L - 1];
       float* db = grad + A.b_off[L - 1];
-      for (int e = tid; e < d_out * K; e += NTC) {
-        const int o = e / K, k = e - o * K;
+      // one task per (output, input neuron) and one per output bias (k == K)
+      for (int e = tid; e < d_out * (K + 1); e += NTC) {
+        const int o = e / (K + 1), k = e - o * (K + 1);
         float sum = 0.f;
-        for (int r = 0; r < R; ++r) sum = fmaf(gybuf[r * MAX_OUT + o], P1[r * LDS + k], sum);
-        dW[(int64_t)o * K + k] = first ? sum : dW[(int64_t)o * K + k] + sum;
-      }
-      for (int o = tid; o < d_out; o += NTC) {
-        float sum = 0.f;
-        for (int r = 0; r < R; ++r)
-          if (row_v[r]) sum += gybuf[r * MAX_OUT + o];
-        db[o] = first ? sum : db[o] + sum;
+        if (k < K) {
+          for (int r = 0; r < R; ++r) sum = fmaf(gybuf[r * MAX_OUT + o], P1[r * LDS + k], sum);
+          dW[(int64_t)o * K + k] = first ? sum : dW[(int64_t)o * K + k] + sum;
+        } else {
+          for (int r = 0; r < R; ++r)
+            if (row_v[r]) sum += gybuf[r * MAX_OUT + o];
+          db[o] = first ? sum : db[o] + sum;
+        }
       }
       __syncthreads();
-      for (int e = tid; e < RMAX * (kp >> 2); e += NTC) {
-        const int r = e % RMAX, k = (e / RMAX) * 4;
-        float v[4] = {0.f, 0.f, 0.f, 0.f};
-        if (r < R)
-          for (int o = 0; o < d_out; ++o) {
-            const float g = gybuf[r * MAX_OUT + o];
+      // dL/dH_{L-1} = dL/dY . W: a thread keeps one row (its seeds load once), W rows as vectors
+      {
+        const int r = tid % RMAX;
+        float g[MAX_OUT];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-              if (k + i < K) v[i] = fmaf(g, Wl[o * K + k + i], v[i]);
+        for (int o = 0; o < MAX_OUT; ++o) g[o] = o < d_out && r < R ? gybuf[r * MAX_OUT + o] : 0.f;
+        for (int e = tid; e < RMAX * (kp >> 2); e += NTC) {
+          const int k = (e / RMAX) * 4;
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (r < R && k < K) {
+#pragma unroll
+            for (int o = 0; o < MAX_OUT; ++o)
+              if (o < d_out) {
+                const float4 w = ld4(&Wl[o * K + k]);
+                v = make_float4(fmaf(g[o], w.x, v.x), fmaf(g[o], w.y, v.y), fmaf(g[o], w.z, v.z),
+                                fmaf(g[o], w.w, v.w));
+              }
           }
-        st4(&P1[r * LDS + k], make_float4(v[0], v[1], v[2], v[3]));
+          st4(&P1[r * LDS + k], v);
+        }
       }
     }
     __syncthreads();
