@@ -1026,8 +1026,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
                            // Z_{L-1} overlaps the output layer
     cx.issue(opB, scr + (int64_t)(L - 2) * scr_slot, (uint32_t)(128 * p16(A.width[L - 1]) * 4));
 
+    // this CTA's gradient segment, zeroed before the launch; every per-tile sum is added with a
+    // fire-and-forget atomic (one thread owns each address, so the order of the adds is fixed)
     float* grad = A.partial + (int64_t)tile.seg * A.part_stride;
-    const bool first = tile.first_in_seg != 0;
     // ---- output layer backward: dW, db (H_{L-1} in P1), then dL/dH_{L-1} -> P1
     {
       const int K = A.width[L - 1], kp = p16(K);
@@ -1040,11 +1041,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         float sum = 0.f;
         if (k < K) {
           for (int r = 0; r < R; ++r) sum = fmaf(gybuf[r * MAX_OUT + o], P1[r * LDS + k], sum);
-          dW[(int64_t)o * K + k] = first ? sum : dW[(int64_t)o * K + k] + sum;
+          red_add1(&dW[(int64_t)o * K + k], sum);
         } else {
           for (int r = 0; r < R; ++r)
             if (row_v[r]) sum += gybuf[r * MAX_OUT + o];
-          db[o] = first ? sum : db[o] + sum;
+          red_add1(&db[o], sum);
         }
       }
       __syncthreads();
@@ -1134,7 +1135,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
 #pragma unroll
           for (int q = 1; q < NPART; ++q) v += red[640 * q + 128 * c + n];
           float* dst = c == 0 ? &db0[n] : &dW0[n * d_in + (c - 1)];
-          *dst = first ? v : *dst + v;
+          red_add1(dst, v);
         }
         break;
       }
@@ -1198,7 +1199,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           float v = red[m];
 #pragma unroll
           for (int q = 1; q < NPART; ++q) v += red[128 * q + m];
-          db[m] = first ? v : db[m] + v;
+          red_add1(&db[m], v);
         }
       }
       cx.publish();

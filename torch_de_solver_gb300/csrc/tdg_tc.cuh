@@ -136,6 +136,11 @@ __device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
 }
 
+// fire-and-forget add of one float to global memory
+__device__ __forceinline__ void red_add1(float* dst, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" :: "l"(dst), "f"(v) : "memory");
+}
+
 // fire-and-forget vector add of 4 floats to global memory (16-byte aligned)
 __device__ __forceinline__ void red_add4(float* dst, float a, float b, float c, float d) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
