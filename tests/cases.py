@@ -251,3 +251,44 @@ COVERAGE_CASES = {
     'neumann_nn': lambda api, dtype='float32': neumann_nn(api, dtype=dtype),
 }
 GOLDEN_CASES.update(COVERAGE_CASES)
+
+
+# ---- one small autograd problem per compile-time jet class (csrc/tdg_jetcls.h) that the benchmark
+# cases above do not reach: the residual site of each is the class named, so the tensor-core kernel
+# variant of that class (and its compiled jets) runs.
+def class_case(kind, api, n=16, seed=11, dtype='float32'):
+    one_d = kind == 'c4'
+    domain = api.Domain()
+    domain.variable('x', [0, 1], n, dtype=dtype)
+    if not one_d:
+        domain.variable('y', [0, 1], n - 2, dtype=dtype)
+    bnd = api.Conditions()
+    u = lambda c, term: {'coeff': c, 'term': term, 'pow': 1, 'var': 0}
+    if one_d:   # u'' + u = 0, u(0) = 0, u(1) = sin 1
+        bnd.dirichlet({'x': 0}, value=0)
+        bnd.dirichlet({'x': 1}, value=math.sin(1.0))
+        terms = {'d2u/dx2': u(1, [0, 0]), 'u': u(1, [None])}
+    else:
+        bnd.dirichlet({'x': 0, 'y': [0, 1]}, value=lambda g: torch.cos(g[:, 1]))
+        bnd.dirichlet({'x': [0, 1], 'y': 0}, value=lambda g: torch.exp(-g[:, 0]))
+        terms = {
+            'c1': {'du/dx': u(1, [0]), 'u': u(1, [None])},
+            'c2': {'du/dy': u(1, [1]), '0.5u': u(0.5, [None])},
+            'c3': {'du/dx': u(1, [0]), 'du/dy': u(1, [1])},
+            'c6': {'du/dx': u(1, [0]), '-0.1d2u/dy2': u(-0.1, [1, 1])},
+            'c9': {'du/dx': u(1, [0]), 'u*du/dy': {'coeff': 1, 'term': [[None], [1]], 'pow': [1, 1],
+                                                   'var': [0, 0]},
+                   '0.01d3u/dy3': u(0.01, [1, 1, 1])},
+            'c10': {'d2u/dx2': u(1, [0, 0]), '0.5d2u/dxdy': u(0.5, [0, 1]), 'd2u/dy2': u(1, [1, 1])},
+        }[kind]
+    eq = api.Equation()
+    eq.add(terms)
+    net = mlp([1 if one_d else 2, 32, 32, 32, 1], seed)
+    # a small boundary weight: the residual (the compiled jets) dominates loss and gradient
+    return domain, bnd, eq, net, dict(mode='autograd', lambda_operator=1, lambda_bound=0.001)
+
+
+CLASS_CASES = {   # name -> (builder, class of the residual site)
+    f'class_{k}': (lambda api, dtype='float32', k=k: class_case(k, api, dtype=dtype), c)
+    for k, c in (('c1', 1), ('c2', 2), ('c3', 3), ('c4', 4), ('c6', 6), ('c9', 9), ('c10', 10))
+}

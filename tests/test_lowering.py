@@ -74,6 +74,22 @@ def test_site_classes(name):
                 assert c == 0
 
 
+@pytest.mark.parametrize('name', list(cases.CLASS_CASES))
+def test_class_coverage_cases_reach_their_class(name):
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300 import _lib
+    from torch_de_solver_gb300.prepare import lower
+    builder, want = cases.CLASS_CASES[name]
+    d, bc, eq, net, kw = builder(T)
+    kw = dict(kw)
+    mode = kw.pop('mode')
+    ir = lower(d.build(mode), eq.equation_lst, bc.build(d.variable_dict), mode,
+               kw['lambda_operator'], kw['lambda_bound'], kw.get('h', 0.001),
+               d_out=net[-1].out_features)
+    for site in ir.groups[ir.residual_group].sites:
+        assert _lib.site_class(site.streams) == want, site.streams
+
+
 def test_site_class_rejects_unlisted_layouts():
     from torch_de_solver_gb300 import _lib
     assert _lib.site_class([(), (0,), (1,), (0, 1)]) == -1          # mixed derivative alone
