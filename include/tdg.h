@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define TDG_ABI_VERSION 1
+#define TDG_ABI_VERSION 2
 
 #define TDG_MAX_LAYERS 12      /* Linear layers of the MLP */
 #define TDG_MAX_DIN 4          /* input coordinates per point */
@@ -51,6 +51,7 @@ extern "C" {
 #define TDG_MAX_ORDER 3        /* derivative order of one stream */
 #define TDG_MAX_STREAMS 16     /* (site, stream) pairs per row */
 #define TDG_MAX_SITES 16       /* evaluation sites per row */
+#define TDG_MAX_COEFF 16       /* trainable equation coefficients per problem */
 
 typedef enum {
   TDG_OK = 0,
@@ -114,13 +115,18 @@ typedef struct {
 } tdg_factor_desc;
 
 /* term: coeff * product of factors, added to the group's output `output`. coeff_array >= 0 names a
- * per-row coefficient array (n_rows floats) that replaces the scalar coeff. */
+ * per-row coefficient array (n_rows floats) that replaces the scalar coeff. coeff_param >= 0 makes
+ * the coefficient trainable: the term's coefficient is coeff * theta, theta the problem's parameter
+ * n_mlp + coeff_param (n_mlp = the MLP's parameter count), and the gradient gets d loss / d theta
+ * at the same index (inverse problems: an nn.Parameter coefficient of the reference,
+ * tedeous/solution.py:96-108). */
 typedef struct {
   int32_t factor_first;
   int32_t n_factors;
   int32_t output;
   int32_t coeff_array;
   float coeff;
+  int32_t coeff_param;
 } tdg_term_desc;
 
 /* a group of rows sharing one site/stream layout and one operator program. Output o of row i is
@@ -158,10 +164,11 @@ typedef struct {
   const int64_t* array_len;                         /* element counts of arrays[] */
   int32_t precision;  /* tdg_precision */
   int32_t form;       /* tdg_form */
+  int32_t n_coeff_params;   /* trainable coefficients per problem, stored after the MLP's parameters */
 } tdg_problem_desc;
 
 typedef struct {
-  int64_t n_params;           /* parameters of one problem */
+  int64_t n_params;           /* parameters of one problem: the MLP's, then the trainable coefficients */
   int64_t workspace_bytes;    /* device memory owned by the plan */
   int32_t n_tiles;
   int32_t n_ctas;

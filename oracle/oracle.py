@@ -109,6 +109,15 @@ def unify(equation):
     return equation
 
 
+def _restore_params(prepared, original):
+    """Trainable (nn.Parameter) coefficients go back into the copied operator, so that the loss
+    reaches the caller's parameters (tedeous/solution.py:91-107, _operator_coeff)."""
+    for key, term in original.items():
+        if isinstance(term['coeff'], torch.nn.Parameter):
+            prepared[key]['coeff'] = term['coeff']
+    return prepared
+
+
 def _bnd_grid(bnd, variable_dict, dtype):
     """Boundary subgrid of one condition (tedeous/data.py:241-286)."""
     if isinstance(bnd, torch.Tensor):
@@ -278,7 +287,7 @@ class Problem:
         self.inner_order, self.boundary_order = inner_order, boundary_order
         self.lambda_operator, self.lambda_bound = lambda_operator, lambda_bound
         ops = equation.equation_lst
-        self.equations = [unify(deepcopy(e)) for e in ops]
+        self.equations = [_restore_params(unify(deepcopy(e)), e) for e in ops]
         self.bconds = build_conditions(conditions.conditions_lst, domain.variable_dict)
         self.nvars = self.grid.shape[1]
         if mode == 'NN':
@@ -301,6 +310,11 @@ class Problem:
     def _coeff_nn(self, coeff, pts):
         if isinstance(coeff, (int, float)):
             return coeff
+        if isinstance(coeff, torch.nn.Parameter):
+            # a trainable scalar; the reference indexes it like a per-point tensor here
+            # (tedeous/input_preprocessing.py:285-288), which fails, so 'NN' mode with trainable
+            # coefficients is an extension checked only against this restatement
+            return coeff
         if isinstance(coeff, torch.Tensor):
             return coeff[bndpos(self.grid, pts)].reshape(-1, 1)
         if callable(coeff):
@@ -310,7 +324,7 @@ class Problem:
     def _prep_nn(self, eq, pts, ptype):
         label = self.inner_order if ptype == 'central' else self.boundary_order
         out = []
-        for term in unify(deepcopy(eq)).values():
+        for term in _restore_params(unify(deepcopy(eq)), eq).values():
             key = list(term.keys())[1]
             factors = []
             for j, d in enumerate(term[key]):
@@ -325,7 +339,9 @@ class Problem:
         for term in eq.values():
             key = list(term.keys())[1]
             c = term['coeff']
-            if isinstance(c, torch.Tensor):
+            if isinstance(c, torch.nn.Parameter):
+                pass   # used as it is, shape (1,) (tedeous/solution.py:91-107 puts it back)
+            elif isinstance(c, torch.Tensor):
                 c = c.reshape(-1, 1)
             elif not isinstance(c, (int, float)) and not callable(c):
                 raise NameError('"coeff" should be: torch.Tensor or callable or int or float!')

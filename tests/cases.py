@@ -245,10 +245,48 @@ def neumann_nn(api, n=14, seed=5, dtype='float32'):
     return domain, bnd, eq, net, dict(mode='NN', lambda_operator=1, lambda_bound=10, h=1.0 / n)
 
 
+def register_coefficients(net, values):
+    """Trainable equation coefficients as parameters of the network, the way
+    tedeous.models.parameter_registr (tedeous/models.py:183-196) registers them."""
+    dtype = next(net.parameters()).dtype
+    for name, v in values.items():
+        # float32 first, like parameter_registr's .float(), so that fp32 and fp64 runs start equal
+        net.register_parameter(name, torch.nn.Parameter(
+            torch.tensor([v], dtype=torch.float32).to(dtype)))
+
+
+def inverse_burgers_ag(api, n=20, seed=6, dtype='float32', n_data=200, mode='autograd'):
+    """Inverse Burgers problem u_t + lam1 u u_x + lam2 u_xx = 0 with lam1, lam2 trainable,
+    fitted to u data at seeded random points (the setup of
+    examples/examples_burgers/example_burgers_1d_inverse.py:19-97, synthetic data
+    u = -sin(pi x) exp(-t) instead of its data file)."""
+    domain = api.Domain()
+    domain.variable('x', [-1, 1], n, dtype=dtype)
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    gen = torch.Generator().manual_seed(seed)
+    pts = torch.rand(n_data, 2, generator=gen, dtype=torch.float64) * torch.tensor([2.0, 1.0]) \
+        - torch.tensor([1.0, 0.0])
+    val = (-torch.sin(np.pi * pts[:, 0]) * torch.exp(-pts[:, 1])).reshape(-1, 1)
+    bnd.data(bnd=pts.float(), operator=None, value=val.float())
+    net = mlp([2, 32, 32, 32, 1], seed, getattr(torch, dtype))
+    register_coefficients(net, {'lam1': 2.0, 'lam2': 0.2})
+    eq = api.Equation()
+    eq.add({'du/dt**1': {'coeff': 1., 'du/dt': [1], 'pow': 1, 'var': 0},
+            '+u*du/dx': {'coeff': net.lam1, 'u*du/dx': [[None], [0]], 'pow': [1, 1],
+                         'var': [0, 0]},
+            '-mu*d2u/dx2': {'coeff': net.lam2, 'd2u/dx2': [0, 0], 'pow': 1, 'var': 0}})
+    kw = dict(mode=mode, lambda_operator=1, lambda_bound=100)
+    if mode == 'NN':
+        kw['h'] = 2.0 / n
+    return domain, bnd, eq, net, kw
+
+
 COVERAGE_CASES = {
     'neumann_ag': lambda api, dtype='float32': neumann_ag(api, dtype=dtype),
     'robin_data_ag': lambda api, dtype='float32': robin_data_ag(api, dtype=dtype),
     'neumann_nn': lambda api, dtype='float32': neumann_nn(api, dtype=dtype),
+    'inverse_burgers_ag': lambda api, dtype='float32': inverse_burgers_ag(api, dtype=dtype),
 }
 GOLDEN_CASES.update(COVERAGE_CASES)
 

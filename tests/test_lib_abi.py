@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.tdg_abi_version() == 1
+    assert lib.tdg_abi_version() == _lib.ABI_VERSION == 2
 
 
 def test_struct_sizes_match_header():
@@ -32,6 +32,7 @@ def test_struct_sizes_match_header():
     assert ctypes.sizeof(_lib.GroupDesc) == 48
     assert ctypes.sizeof(_lib.SiteDesc) == 28
     assert ctypes.sizeof(_lib.SlotDesc) == 24
+    assert ctypes.sizeof(_lib.TermDesc) == 24
 
 
 def test_invalid_arguments_return_status():

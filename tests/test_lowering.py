@@ -108,3 +108,60 @@ def test_unsupported_features_raise():
         lower(d.build('autograd'), eq.equation_lst, bc.build(d.variable_dict), 'autograd', 1, 1)
     with pytest.raises(NotImplementedError):
         d.build('mat')
+
+
+def _lower_case(T, builder, **kw_case):
+    from torch_de_solver_gb300.prepare import lower
+    d, bc, eq, net, kw = builder(T, **kw_case)
+    mode = kw['mode']
+    ir = lower(d.build(mode), eq.equation_lst, bc.build(d.variable_dict), mode,
+               kw['lambda_operator'], kw['lambda_bound'], kw.get('h', 0.001), d_out=1)
+    return ir, net
+
+
+@pytest.mark.parametrize('mode', ['autograd', 'NN'])
+def test_trainable_coefficients_lower_to_parameter_slots(mode):
+    """nn.Parameter coefficients keep their identity through the lowering's copy and become
+    coefficient slots in first-use order; every other coefficient stays a constant."""
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300.prepare import CoeffParam
+    ir, net = _lower_case(T, cases.inverse_burgers_ag, n=8, mode=mode)
+    assert [id(p) for p in ir.coeff_params] == [id(net.lam1), id(net.lam2)]
+    res = ir.groups[ir.residual_group]
+    marks = [(c.index, c.scale) for c, _, _ in res.terms if isinstance(c, CoeffParam)]
+    assert sorted(set(i for i, _ in marks)) == [0, 1]
+    assert all(s == 1.0 for _, s in marks)
+    for grp in ir.groups:
+        if grp is not res:
+            assert not any(isinstance(c, CoeffParam) for c, _, _ in grp.terms)
+
+
+def test_trainable_coefficient_in_boundary_operator_raises():
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300.prepare import lower
+    d, bc, eq, net, kw = cases.neumann_ag(T, n=8)
+    cases.register_coefficients(net, {'k': 1.5})
+    bc.conditions_lst[1]['bop']['du/dx']['coeff'] = net.k
+    with pytest.raises(NotImplementedError, match='boundary operators'):
+        lower(d.build('autograd'), eq.equation_lst, bc.build(d.variable_dict), 'autograd', 1, 1)
+
+
+def test_device_parameter_order_and_optimizer_order():
+    """The device buffer holds the Linear layers first, then the coefficients, while
+    Module.parameters() lists the registered coefficients first; the optimizer gets the buffer's
+    order, and a parameter that is neither is refused."""
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300.optimizer import _in_buffer_order
+    from torch_de_solver_gb300.solution import device_parameters, flatten_parameters
+    ir, net = _lower_case(T, cases.inverse_burgers_ag, n=8)
+    names = [n for n, _ in net.named_parameters()]
+    assert names[:2] == ['lam1', 'lam2']
+    params = device_parameters(net, ir.coeff_params)
+    assert params[-2] is net.lam1 and params[-1] is net.lam2 and params[0] is net[0].weight
+    flat = flatten_parameters(params, torch.device('cpu'))
+    assert flat.numel() == sum(p.numel() for p in net.parameters())
+    assert float(flat[-2]) == 2.0 and abs(float(flat[-1]) - 0.2) < 1e-7
+    assert [id(p) for p in _in_buffer_order(net.parameters())] == [id(p) for p in params]
+    net.register_parameter('stray', torch.nn.Parameter(torch.zeros(3)))
+    with pytest.raises(NotImplementedError):
+        device_parameters(net, ir.coeff_params)

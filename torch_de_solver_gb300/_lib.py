@@ -18,6 +18,8 @@ MAX_WIDTH = 128
 MAX_ORDER = 3
 MAX_STREAMS = 16
 MAX_SITES = 16
+MAX_COEFF = 16
+ABI_VERSION = 2
 
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_SHAPE, ERR_CUDA, ERR_TIMEOUT, ERR_NOMEM = range(7)
 PREC = {'fp32': 0, 'tf32': 1, '3xtf32': 2, 'bf16': 3}
@@ -49,7 +51,7 @@ class FactorDesc(ctypes.Structure):
 
 class TermDesc(ctypes.Structure):
     _fields_ = [('factor_first', i32), ('n_factors', i32), ('output', i32), ('coeff_array', i32),
-                ('coeff', f32)]
+                ('coeff', f32), ('coeff_param', i32)]
 
 
 class GroupDesc(ctypes.Structure):
@@ -72,7 +74,7 @@ class ProblemDesc(ctypes.Structure):
                 ('n_parts', i32), ('parts', ctypes.POINTER(PartDesc)),
                 ('n_slots', i32), ('slots', ctypes.POINTER(SlotDesc)),
                 ('n_arrays', i32), ('arrays', ctypes.POINTER(vp)), ('array_len', ctypes.POINTER(i64)),
-                ('precision', i32), ('form', i32)]
+                ('precision', i32), ('form', i32), ('n_coeff_params', i32)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -126,7 +128,7 @@ def load():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.tdg_abi_version() != 1:
+    if lib.tdg_abi_version() != ABI_VERSION:
         raise ImportError('libtdg.so ABI version mismatch')
     _lib = lib
     return lib

@@ -292,6 +292,7 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
   double* slot_acc = reinterpret_cast<double*>(
       (reinterpret_cast<uintptr_t>(Gs + 1) + 15) & ~uintptr_t(15));
   double* wred = slot_acc + MAX_SLOTS;             // [NT/32][MAX_OUT]
+  float* cred = reinterpret_cast<float*>(wred + NT / 32 * MAX_OUT);   // [NT/32][TDG_MAX_COEFF]
 
   const int tid = threadIdx.x;
   const int cta = blockIdx.x;
@@ -398,6 +399,9 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     float err2[MAX_OUT];
 #pragma unroll
     for (int o = 0; o < MAX_OUT; ++o) err2[o] = 0.f;
+    float gc[TDG_MAX_COEFF];   // this point's d loss / d trainable coefficient
+#pragma unroll
+    for (int k = 0; k < TDG_MAX_COEFF; ++k) gc[k] = 0.f;
     if (tid < T) {
       const int p = tid;
       const bool valid = p < nvalid;
@@ -406,7 +410,8 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       for (int o = 0; o < MAX_OUT; ++o) outv[o] = 0.f;
       for (int t = 0; t < G.n_terms; ++t) {
         const DevTerm& tm = G.terms[t];
-        const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+        const float c = tm.coeff_param >= 0 ? tm.coeff * __ldg(&prm[A.coeff_off + tm.coeff_param])
+                        : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
         float prod = 1.f;
         for (int f = 0; f < tm.n_factors; ++f) {
           const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -434,9 +439,10 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       if (A.do_grad) {
         for (int t = 0; t < G.n_terms; ++t) {
           const DevTerm& tm = G.terms[t];
-          const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+          const float c = tm.coeff_param >= 0 ? tm.coeff * __ldg(&prm[A.coeff_off + tm.coeff_param])
+                          : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
           const float dt = seed[tm.output] * c;
-          if (dt == 0.f) continue;
+          if (dt == 0.f && tm.coeff_param < 0) continue;
           float F[MAX_TERM_FACTORS];
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -446,6 +452,14 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
               v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
             }
             F[f] = v;
+          }
+          if (tm.coeff_param >= 0) {   // d loss / d coefficient: seed * scale * product
+            float prod = 1.f;
+            for (int f = 0; f < tm.n_factors; ++f) prod *= pow_f(F[f], G.factors[tm.factor_first + f].power);
+#pragma unroll
+            for (int k = 0; k < TDG_MAX_COEFF; ++k)
+              if (k == tm.coeff_param) gc[k] += seed[tm.output] * tm.coeff * prod;
+            if (dt == 0.f) continue;
           }
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -475,6 +489,16 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
         for (int w = 0; w < NT / 32; ++w) s += wred[w * MAX_OUT + tid];
         slot_acc[G.slot_first + tid] += s;
       }
+      if (A.do_grad && A.n_coeff > 0) {   // coefficient gradients: warp shuffle, warps in order below
+#pragma unroll
+        for (int k = 0; k < TDG_MAX_COEFF; ++k) {
+          if (k >= A.n_coeff) break;
+          float v = gc[k];
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+          if (lane == 0) cred[warp * TDG_MAX_COEFF + k] = v;
+        }
+      }
     }
     if (!A.do_grad) continue;
     __syncthreads();
@@ -482,6 +506,12 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     // ---- backward: gybuf holds dL/dY of every (point, stream) row
     float* grad = A.partial + (int64_t)tile.seg * A.part_stride;
     const bool first = tile.first_in_seg != 0;
+    if (tid < A.n_coeff) {   // every coefficient slot of the segment, written on its first tile
+      float s = 0.f;
+      for (int w = 0; w < NT / 32; ++w) s += cred[w * TDG_MAX_COEFF + tid];
+      float* dst = grad + A.coeff_off + tid;
+      *dst = first ? s : *dst + s;
+    }
     // output layer: dW, db, and dL/dH of the last hidden layer into hout
     {
       const int K = A.width[L - 1];

@@ -1,5 +1,5 @@
 // Tensor-core fused kernel: shared-memory size, the bounded-wait self-test and the dispatch to
-// the precision variants (instantiated in tdg_tc_tf32.cu, tdg_tc_bf16.cu, tdg_tc_3x.cu).
+// the variants of each precision and main site class (instantiated from tdg_tc_inst.cu).
 #include "tdg_fused_tc.cuh"
 
 namespace tdg {

@@ -37,7 +37,8 @@ constexpr int PB_W0 = PB_HB + (TDG_MAX_LAYERS - 2) * TDG_MAX_WIDTH;
 constexpr int PB_B0 = PB_W0 + TDG_MAX_WIDTH * TDG_MAX_DIN;
 constexpr int PB_WL = PB_B0 + TDG_MAX_WIDTH;
 constexpr int PB_BL = PB_WL + TDG_MAX_DOUT * TDG_MAX_WIDTH;
-constexpr int PBUF = PB_BL + TDG_MAX_DOUT;
+constexpr int PB_CF = PB_BL + TDG_MAX_DOUT;                     // trainable coefficients
+constexpr int PBUF = PB_CF + TDG_MAX_COEFF;
 
 __device__ __forceinline__ int p16(int w) { return (w + 15) & ~15; }
 
@@ -768,6 +769,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         for (int n = tid; n < A.width[1]; n += NTC) pbuf[PB_B0 + n] = pp[A.b_off[0] + n];
         for (int e = tid; e < d_out * A.width[L - 1]; e += NTC) pbuf[PB_WL + e] = pp[A.w_off[L - 1] + e];
         for (int o = tid; o < d_out; o += NTC) pbuf[PB_BL + o] = pp[A.b_off[L - 1] + o];
+        for (int k = tid; k < A.n_coeff; k += NTC) pbuf[PB_CF + k] = pp[A.coeff_off + k];
       }
       __syncthreads();
     }
@@ -956,7 +958,8 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const int p = e % T, t = e / T;
         const DevTerm& tm = G.terms[t];
         const bool valid = p < nvalid;
-        const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+        const float c = tm.coeff_param >= 0 ? tm.coeff * pbuf[PB_CF + tm.coeff_param]
+                        : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
         float prod = 1.f;
         for (int f = 0; f < tm.n_factors; ++f) {
           const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -995,9 +998,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           const int p = e % T, t = e / T;
           const DevTerm& tm = G.terms[t];
           const bool valid = p < nvalid;
-          const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
-          const float dt = seedv[tm.output * RMAX + p] * c;
-          if (dt == 0.f) continue;
+          const float c = tm.coeff_param >= 0 ? tm.coeff * pbuf[PB_CF + tm.coeff_param]
+                          : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+          const float sd = seedv[tm.output * RMAX + p];
+          const float dt = sd * c;
+          if (dt == 0.f && tm.coeff_param < 0) continue;
           float F[MAX_TERM_FACTORS];
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -1008,6 +1013,12 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             }
             F[f] = v;
           }
+          if (tm.coeff_param >= 0) {   // d loss / d coefficient: seed * scale * product (term values are dead)
+            float prod = 1.f;
+            for (int f = 0; f < tm.n_factors; ++f) prod *= powf_(F[f], G.factors[tm.factor_first + f].power);
+            tv[t * RMAX + p] = sd * tm.coeff * prod;
+            if (dt == 0.f) continue;
+          }
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
             float d = dt * dpowf_(F[f], fc.power);
@@ -1017,6 +1028,20 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
               const DevPart& pt = G.parts[fc.part_first + u];
               atomicAdd(&gybuf[(pt.stream * T + p) * MAX_OUT + fc.var], d * pt.weight);
             }
+          }
+        }
+        if (A.n_coeff > 0) {   // one thread per coefficient: its terms and points in order
+          __syncthreads();
+          float* cgrad = A.partial + (int64_t)tile.seg * A.part_stride + A.coeff_off;
+          for (int k = tid; k < A.n_coeff; k += NTC) {
+            float sum = 0.f;
+            bool used = false;
+            for (int t = 0; t < nt; ++t)
+              if (G.terms[t].coeff_param == k) {
+                used = true;
+                for (int p = 0; p < T; ++p) sum += tv[t * RMAX + p];
+              }
+            if (used) red_add1(&cgrad[k], sum);
           }
         }
       }

@@ -37,6 +37,7 @@ struct DevPull {
 struct DevTerm {
   int16_t factor_first, n_factors, output, coeff_array;
   float coeff;
+  int16_t coeff_param, pad;   // trainable coefficient index (-1: none)
 };
 
 struct DevFactor {
@@ -85,6 +86,8 @@ struct FusedArgs {
   const float* const* arrays;         // device table of device pointers
   const float* params;                // n_problems x n_params
   int64_t n_params;                   // per problem
+  int64_t coeff_off;                  // the trainable coefficients' offset within a problem's params
+  int32_t n_coeff;                    // trainable coefficients per problem
   int64_t part_stride;                // floats per gradient segment (n_params rounded up to 4)
   float* partial;                     // n_segments x part_stride
   double* slot_partial;               // n_ctas x n_slots
@@ -100,7 +103,8 @@ struct FusedArgs {
 // shared-memory bytes of the fused FP32 kernel
 constexpr size_t fused_smem_bytes() {
   return sizeof(float) * (3 * RMAX * LDS + 2 * RMAX * MAX_OUT + RMAX * TDG_MAX_DIN)
-         + sizeof(DevGroup) + sizeof(double) * (MAX_SLOTS + NT / 32 * MAX_OUT) + 64;
+         + sizeof(DevGroup) + sizeof(double) * (MAX_SLOTS + NT / 32 * MAX_OUT)
+         + sizeof(float) * (NT / 32) * TDG_MAX_COEFF + 64;
 }
 
 cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s);
@@ -132,6 +136,8 @@ struct PlainArgs {
   const float* params;
   float* grad;
   int64_t n_params;
+  int64_t coeff_off;                // the trainable coefficients' offset within a problem's params
+  int32_t n_coeff;
   int32_t n_problems;
   int32_t n_layers;
   int32_t width[TDG_MAX_LAYERS + 1];

@@ -231,19 +231,24 @@ __global__ void plain_output(const DevGroup* __restrict__ G, const float* __rest
 }
 
 // operator program per point: outputs, squared errors into FP64 slot sums, seeds dL/dY
+// (trainable coefficients: values cf[k], gradients accumulated into cgrad[k], k < n_coeff)
 __global__ void plain_program(const DevGroup* __restrict__ G, const float* const* __restrict__ arrays,
                               const float* __restrict__ Y, float* __restrict__ GY, int d_out,
                               double* __restrict__ slot_sum, float* __restrict__ outputs,
-                              int do_grad) {
+                              int do_grad, const float* __restrict__ cf, float* __restrict__ cgrad,
+                              int n_coeff) {
   const int n = G->n_rows, n_out = G->n_outputs;
   __shared__ double red[MAX_OUT];
+  __shared__ float cred[TDG_MAX_COEFF];
   if (threadIdx.x < MAX_OUT) red[threadIdx.x] = 0.0;
+  if (threadIdx.x < TDG_MAX_COEFF) cred[threadIdx.x] = 0.f;
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float outv[MAX_OUT] = {};
     for (int t = 0; t < G->n_terms; ++t) {
       const DevTerm& tm = G->terms[t];
-      const float c = tm.coeff_array >= 0 ? arrays[tm.coeff_array][i] : tm.coeff;
+      const float c = tm.coeff_param >= 0 ? tm.coeff * cf[tm.coeff_param]
+                      : tm.coeff_array >= 0 ? arrays[tm.coeff_array][i] : tm.coeff;
       float prod = 1.f;
       for (int f = 0; f < tm.n_factors; ++f) {
         const DevFactor& fc = G->factors[tm.factor_first + f];
@@ -267,7 +272,8 @@ __global__ void plain_program(const DevGroup* __restrict__ G, const float* const
     if (!do_grad) continue;
     for (int t = 0; t < G->n_terms; ++t) {
       const DevTerm& tm = G->terms[t];
-      const float c = tm.coeff_array >= 0 ? arrays[tm.coeff_array][i] : tm.coeff;
+      const float c = tm.coeff_param >= 0 ? tm.coeff * cf[tm.coeff_param]
+                      : tm.coeff_array >= 0 ? arrays[tm.coeff_array][i] : tm.coeff;
       const float dt = seed[tm.output] * c;
       float F[MAX_TERM_FACTORS];
       for (int f = 0; f < tm.n_factors; ++f) {
@@ -278,6 +284,11 @@ __global__ void plain_program(const DevGroup* __restrict__ G, const float* const
           v = fmaf(Y[((int64_t)pt.stream * n + i) * d_out + fc.var], pt.weight, v);
         }
         F[f] = v;
+      }
+      if (tm.coeff_param >= 0) {   // d loss / d coefficient: seed * scale * product
+        float prod = 1.f;
+        for (int f = 0; f < tm.n_factors; ++f) prod *= pw(F[f], G->factors[tm.factor_first + f].power);
+        atomicAdd(&cred[tm.coeff_param], seed[tm.output] * tm.coeff * prod);
       }
       for (int f = 0; f < tm.n_factors; ++f) {
         const DevFactor& fc = G->factors[tm.factor_first + f];
@@ -293,6 +304,7 @@ __global__ void plain_program(const DevGroup* __restrict__ G, const float* const
   }
   __syncthreads();
   if (threadIdx.x < n_out) atomicAdd(&slot_sum[G->slot_first + threadIdx.x], red[threadIdx.x]);
+  if (do_grad && threadIdx.x < n_coeff) atomicAdd(&cgrad[threadIdx.x], cred[threadIdx.x]);
 }
 
 // output layer backward: dL/dH[r][k] = sum_o GY[r][o] W[o][k]
@@ -423,7 +435,8 @@ cudaError_t run_plain(const PlainArgs& P, cudaStream_t s) {
     const int KL = P.width[L - 1];
     plain_output<<<grid_for(rows * d_out), PT, 0, s>>>(G, Hl[L - 1], prm + P.w_off[L - 1], prm + P.b_off[L - 1], KL, d_out, P.y);
     if ((e = cudaMemsetAsync(P.gy, 0, sizeof(float) * rows * d_out, s)) != cudaSuccess) return e;
-    plain_program<<<grid_for(n), PT, 0, s>>>(G, P.arrays, P.y, P.gy, d_out, P.slot_sum, P.outputs, P.do_grad);
+    plain_program<<<grid_for(n), PT, 0, s>>>(G, P.arrays, P.y, P.gy, d_out, P.slot_sum, P.outputs, P.do_grad,
+                                             prm + P.coeff_off, grad + P.coeff_off, P.n_coeff);
     count_launch(2);
     if (!P.do_grad) continue;
     // backward

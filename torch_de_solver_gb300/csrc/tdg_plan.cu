@@ -55,6 +55,8 @@ struct tdg_plan {
   int width[TDG_MAX_LAYERS + 1] = {0};
   int64_t w_off[TDG_MAX_LAYERS] = {0}, b_off[TDG_MAX_LAYERS] = {0};
   int64_t n_params = 0, part_stride = 0;
+  int64_t coeff_off = 0;   // the trainable coefficients follow the MLP's parameters
+  int n_coeff = 0;
   int n_problems = 0, n_slots = 0, n_tiles = 0, n_ctas = 0, n_segments = 0, max_streams = 0;
   int precision = 0, form = 0;
   int cls_main = 0;   // the tensor-core kernel variant: the site class with the most rows
@@ -303,6 +305,11 @@ tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d
     T.output = (int16_t)td.output;
     T.coeff_array = (int16_t)td.coeff_array;
     T.coeff = td.coeff;
+    if (td.coeff_param >= d.n_coeff_params || td.coeff_param < -1)
+      return fail(TDG_ERR_INVALID, "term coefficient parameter %d out of range", td.coeff_param);
+    if (td.coeff_param >= 0 && td.coeff_array >= 0)
+      return fail(TDG_ERR_INVALID, "a term's coefficient is either trainable or a per-row array");
+    T.coeff_param = (int16_t)td.coeff_param;
     for (int f = 0; f < td.n_factors; ++f) {
       const tdg_factor_desc& fd = d.factors[td.factor_first + f];
       if (nf >= MAX_FACTORS) return fail(TDG_ERR_UNSUPPORTED, "too many factors in a group");
@@ -406,6 +413,13 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     p->b_off[l] = off;
     off += d.mlp.width[l + 1];
   }
+  if (d.n_coeff_params < 0 || d.n_coeff_params > TDG_MAX_COEFF) {
+    free_plan(p);
+    return fail(TDG_ERR_UNSUPPORTED, "%d trainable coefficients (0..%d)", d.n_coeff_params, TDG_MAX_COEFF);
+  }
+  p->coeff_off = off;
+  p->n_coeff = d.n_coeff_params;
+  off += d.n_coeff_params;
   p->n_params = off;
   p->part_stride = (off + 3) / 4 * 4;
   p->n_problems = d.n_problems;
@@ -585,6 +599,8 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
   a.arrays = p->d_arrays;
   a.params = params;
   a.n_params = p->n_params;
+  a.coeff_off = p->coeff_off;
+  a.n_coeff = p->n_coeff;
   a.part_stride = p->part_stride;
   a.partial = p->d_partial;
   a.slot_partial = p->d_slot_partial;
@@ -605,6 +621,8 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
     pa.params = params;
     pa.grad = grad;
     pa.n_params = p->n_params;
+    pa.coeff_off = p->coeff_off;
+    pa.n_coeff = p->n_coeff;
     pa.n_problems = p->n_problems;
     pa.n_layers = p->n_layers;
     for (int l = 0; l <= p->n_layers; ++l) pa.width[l] = p->width[l];

@@ -102,7 +102,9 @@ class Model:
         self.min_loss, _ = self.solution_cls.evaluate()
         self.cur_loss = self.min_loss
         print('[{}] initial (min) loss is {}'.format(datetime.datetime.now(), self.min_loss.item()))
-        fused = (isinstance(self.optimizer, FusedAdam) and optimizer.gamma is None
+        fused = (isinstance(self.optimizer, FusedAdam)
+                 and self.optimizer._flat.data_ptr() == self.solution_cls.flat.data_ptr()
+                 and optimizer.gamma is None
                  and optimizer.cosine_scheduler_patience is None and not self.normalized_loss_stop)
         self._graph = None
         n_eager = 0
@@ -142,7 +144,7 @@ class BatchedModel:
     def compile(self, mode: str, lambda_operator, lambda_bound, h: float = 0.001,
                 inner_order: str = '1', boundary_order: str = '2', precision: str = 'fp32'):
         from .prepare import lower
-        from .solution import DevicePlan, mlp_widths
+        from .solution import DevicePlan, device_parameters, flatten_parameters, mlp_widths
         if not torch.cuda.is_available():
             raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
         dev = torch.device('cuda', torch.cuda.current_device())
@@ -159,16 +161,11 @@ class BatchedModel:
         self.irs = irs
         self.plan = DevicePlan(irs, widths, dev, precision)
         P = self.plan.n_params
-        self.flat = torch.cat([torch.cat([p.detach().reshape(-1).float() for p in m.net.parameters()])
-                               for m in self.models]).to(dev)
-        with torch.no_grad():
-            for i, m in enumerate(self.models):
-                m.net.to(dev)
-                off = i * P
-                for p in m.net.parameters():
-                    n = p.numel()
-                    p.data = self.flat[off:off + n].view(p.shape)
-                    off += n
+        for m in self.models:
+            m.net.to(dev)
+        self.params = [device_parameters(m.net, ir.coeff_params) for m, ir in zip(self.models, irs)]
+        self.flat = flatten_parameters([p for ps in self.params for p in ps], dev)
+        assert self.flat.numel() == P * len(self.models)
         self.grad = torch.zeros_like(self.flat)
         self.loss = torch.zeros(2 * len(self.models), dtype=torch.float64, device=dev)
         self.outputs = torch.zeros(max(1, self.plan.n_outputs_total), device=dev)

@@ -13,6 +13,18 @@ from torch.optim.lr_scheduler import CosineAnnealingWarmRestarts, ExponentialLR
 from . import _lib
 
 
+def _in_buffer_order(params):
+    """Parameters that are views of one buffer, ordered by their place in it (the device path
+    puts a network's trainable equation coefficients after its layers, while
+    Module.parameters() lists a module's own registered parameters first)."""
+    params = list(params)
+    if params and all(isinstance(p, torch.Tensor) for p in params):
+        st = {p.data.untyped_storage().data_ptr() for p in params}
+        if len(st) == 1:
+            return sorted(params, key=lambda p: p.data.storage_offset())
+    return params
+
+
 def _flat_of(params):
     """The flat buffer the parameters are views of, or None."""
     if not params:
@@ -222,12 +234,15 @@ class Optimizer:
                                       f'device path (Adam, AdamW, SGD, LBFGS, RMSprop are)')
         if mode not in ('NN', 'autograd'):
             raise NotImplementedError(f'mode {mode!r}')
-        if self.optimizer == 'Adam':
-            opt = FusedAdam(model.parameters(), **self.params)
+        params = _in_buffer_order(model.parameters())
+        if self.optimizer == 'Adam' and _flat_of(params) is not None:
+            opt = FusedAdam(params, **self.params)
+        elif self.optimizer == 'Adam':   # parameters with gaps (a coefficient outside the network)
+            opt = torch.optim.Adam(params, **self.params)
         elif self.optimizer == 'LBFGS' and self.params.get('line_search_fn') is None:
-            opt = LBFGS64(model.parameters(), **self.params)
+            opt = LBFGS64(params, **self.params)
         else:
-            opt = names[self.optimizer](model.parameters(), **self.params)
+            opt = names[self.optimizer](params, **self.params)
         if self.gamma is not None:
             self.scheduler = ExponentialLR(opt, gamma=self.gamma)
         if self.cosine_scheduler_patience is not None:

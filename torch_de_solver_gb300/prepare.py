@@ -162,6 +162,7 @@ class ProblemIR:
     def __init__(self, d_in, d_out):
         self.d_in, self.d_out = d_in, d_out
         self.arrays = []              # float32 CPU tensors (flattened on upload)
+        self.coeff_params = []        # trainable coefficients (nn.Parameter), in first-use order
         self.groups = []
         self.slots = []               # (problem, weight, weight_normalized)
         self.residual_group = None
@@ -172,14 +173,46 @@ class ProblemIR:
         self.max_len = 0
         self.n_residual_rows = 0
 
+    def coeff_index(self, param):
+        """Slot of a trainable coefficient (one per distinct nn.Parameter)."""
+        for i, q in enumerate(self.coeff_params):
+            if q is param:
+                return i
+        self.coeff_params.append(param)
+        return len(self.coeff_params) - 1
+
     def add_array(self, t):
         self.arrays.append(t.detach().cpu().to(torch.float32).contiguous())
         return len(self.arrays) - 1
 
 
+class CoeffParam:
+    """A term coefficient scale * theta, theta a trainable scalar (an nn.Parameter of one element,
+    as tedeous.models.parameter_registr makes them); `index` is theta's slot in
+    ProblemIR.coeff_params."""
+
+    def __init__(self, index, scale=1.0):
+        self.index = index
+        self.scale = scale
+
+
+def _copy_keeping_params(eq):
+    """Deep copy of an operator dict in which the trainable (nn.Parameter) coefficients stay the
+    caller's objects, so that their gradient reaches them (the reference puts them back after its
+    own copy, tedeous/solution.py:91-107)."""
+    memo = {}
+    for term in eq.values():
+        c = term.get('coeff') if isinstance(term, dict) else None
+        if isinstance(c, torch.nn.Parameter):
+            memo[id(c)] = c
+    return deepcopy(eq, memo)
+
+
 def _check_coeff(coeff):
     if isinstance(coeff, torch.nn.Parameter):
-        raise NotImplementedError('trainable (nn.Parameter) coefficients are not implemented')
+        if coeff.numel() != 1:
+            raise NotImplementedError('a trainable coefficient must be a single value')
+        return
     if isinstance(coeff, (int, float, np.floating, np.integer)) or isinstance(coeff, torch.Tensor) \
             or callable(coeff):
         return
@@ -200,7 +233,7 @@ class Lowering:
         self.inner_order, self.boundary_order = inner_order, boundary_order
         if isinstance(operator, dict):
             operator = [operator]
-        self.equations = [unify_operator(deepcopy(e)) for e in operator]
+        self.equations = [unify_operator(_copy_keeping_params(e)) for e in operator]
         self.bconds = bconds
         self.lambda_operator, self.lambda_bound = lambda_operator, lambda_bound
         self.ir = ProblemIR(grid.shape[1], d_out)
@@ -221,6 +254,8 @@ class Lowering:
     # -- one operator (dict of terms) into a group's terms ------------------------------
     def _coeff(self, coeff, pts, rows_in_grid):
         _check_coeff(coeff)
+        if isinstance(coeff, torch.nn.Parameter):
+            return CoeffParam(self.ir.coeff_index(coeff))
         if isinstance(coeff, torch.Tensor):
             c = coeff.detach().cpu().reshape(-1)
             if rows_in_grid is not None:
@@ -263,6 +298,8 @@ class Lowering:
             return c
         if isinstance(c, float):
             return -c
+        if isinstance(c, CoeffParam):
+            return CoeffParam(c.index, -c.scale)
         self.ir.arrays[c] = -self.ir.arrays[c]
         return c
 
@@ -391,6 +428,11 @@ class Lowering:
         ir = self.ir
         vals = {}     # type -> list of (group or None, positions, n_rows)
         for bc in (self.bconds or []):
+            bop = bc.get('bop')
+            if isinstance(bop, dict) and any(isinstance(term.get('coeff'), torch.nn.Parameter)
+                                             for term in bop.values() if isinstance(term, dict)):
+                raise NotImplementedError('trainable (nn.Parameter) coefficients are implemented '
+                                          'in the equation operator, not in boundary operators')
             t = bc['type']
             if t not in slot_of_type:
                 slot_of_type[t] = None

@@ -16,7 +16,7 @@ import ctypes
 import torch
 
 from . import _lib
-from .prepare import lower
+from .prepare import CoeffParam, lower
 
 
 def mlp_widths(net):
@@ -41,10 +41,22 @@ def mlp_widths(net):
     return widths
 
 
-def flatten_parameters(net, device):
-    """Move `net` to `device` and make its parameters views of one flat float32 buffer
-    (torch.nn.Module.parameters() order: W0, b0, W1, b1, ...)."""
-    params = list(net.parameters())
+def device_parameters(net, coeff_params=()):
+    """The parameters in the order of the device's flat buffer: every Linear layer's weight and
+    bias in layer order, then the equation's trainable coefficients (ProblemIR.coeff_params).
+    Other parameters of `net` have no place on the device path."""
+    lin = [m for m in net.children() if isinstance(m, torch.nn.Linear)]
+    params = [q for m in lin for q in (m.weight, m.bias)] + list(coeff_params)
+    known = set(map(id, params))
+    for name, q in net.named_parameters():
+        if id(q) not in known:
+            raise NotImplementedError(f'parameter {name!r} is neither a Linear weight or bias nor '
+                                      f'a coefficient of the equation')
+    return params
+
+
+def flatten_parameters(params, device):
+    """Make `params` views of one flat float32 buffer on `device`, in the order given."""
     flat = torch.cat([p.detach().reshape(-1).to(device=device, dtype=torch.float32)
                       for p in params])
     off = 0
@@ -56,9 +68,9 @@ def flatten_parameters(net, device):
     return flat
 
 
-def params_are_views(net, flat):
+def params_are_views(params, flat):
     off = 0
-    for p in net.parameters():
+    for p in params:
         if p.data.data_ptr() != flat.data_ptr() + 4 * off or p.dtype != torch.float32:
             return False
         off += p.numel()
@@ -80,6 +92,11 @@ class DevicePlan:
         self.arrays = []
         self.group_out = []          # per problem: list of (group, output offset) in IR order
         out_off = 0
+        n_coeff = {len(ir.coeff_params) for ir in irs}
+        if len(n_coeff) != 1:
+            raise ValueError('the problems of one plan must have the same number of trainable '
+                             'coefficients')
+        self.n_coeff = n_coeff.pop()
         for prob, ir in enumerate(irs):
             base = len(self.arrays)
             self.arrays += [a.to(device).reshape(-1).contiguous() for a in ir.arrays]
@@ -105,9 +122,12 @@ class DevicePlan:
                             parts.append(_lib.PartDesc(site, stream, w))
                         factors.append(_lib.FactorDesc(p_first, len(pl), var, pw))
                     if isinstance(coeff, float):
-                        terms.append(_lib.TermDesc(f_first, len(fl), output, -1, coeff))
+                        terms.append(_lib.TermDesc(f_first, len(fl), output, -1, coeff, -1))
+                    elif isinstance(coeff, CoeffParam):
+                        terms.append(_lib.TermDesc(f_first, len(fl), output, -1, coeff.scale,
+                                                   coeff.index))
                     else:
-                        terms.append(_lib.TermDesc(f_first, len(fl), output, base + coeff, 0.0))
+                        terms.append(_lib.TermDesc(f_first, len(fl), output, base + coeff, 0.0, -1))
                 tgt = -1 if g.target is None else base + g.target
                 groups.append(_lib.GroupDesc(prob, g.n_rows, site_first, len(g.sites), term_first,
                                              len(g.terms), g.n_outputs, slot_base + g.slot_first,
@@ -139,7 +159,7 @@ class DevicePlan:
             mlp, len(irs), len(groups), k['groups'], len(sites), k['sites'], len(streams),
             k['streams'], len(terms), k['terms'], len(factors), k['factors'], len(parts),
             k['parts'], len(slots), k['slots'], len(self.arrays), k['ptrs'], k['lens'],
-            _lib.PREC[precision], _lib.FORM[form])
+            _lib.PREC[precision], _lib.FORM[form], self.n_coeff)
         handle = ctypes.c_void_p()
         with torch.cuda.device(device):
             _lib.check(lib.tdg_plan_create(ctypes.byref(desc), ctypes.byref(handle)),
@@ -220,8 +240,9 @@ class Solution:
         self.ir = lower(grid, operator, bconds, mode, lambda_operator, lambda_bound, h,
                         inner_order, boundary_order, d_out=widths[-1])
         self.model = model.to(self.device)
-        self.flat = flatten_parameters(self.model, self.device)
-        self._shapes = [(p.shape, p.numel()) for p in self.model.parameters()]
+        self.params = device_parameters(self.model, self.ir.coeff_params)
+        self.flat = flatten_parameters(self.params, self.device)
+        self._shapes = [(p.shape, p.numel()) for p in self.params]
         self.plan = DevicePlan([self.ir], widths, self.device, precision, form)
         self._grad = torch.zeros(self.plan.n_params, device=self.device, dtype=torch.float32)
         self._loss_buf = torch.zeros(2, device=self.device, dtype=torch.float64)
@@ -237,11 +258,12 @@ class Solution:
         if mlp_widths(new_model) != self.plan.widths:
             raise ValueError('new model has a different shape')
         self.model = new_model.to(self.device)
-        self.flat = flatten_parameters(self.model, self.device)
+        self.params = device_parameters(self.model, self.ir.coeff_params)
+        self.flat = flatten_parameters(self.params, self.device)
 
     def _sync_params(self):
-        if not params_are_views(self.model, self.flat):
-            self.flat = flatten_parameters(self.model, self.device)
+        if not params_are_views(self.params, self.flat):
+            self.flat = flatten_parameters(self.params, self.device)
 
     # -- evaluation --------------------------------------------------------------------------
     def _launch(self, with_grad):
@@ -253,7 +275,7 @@ class Solution:
     def evaluate(self, save_graph: bool = True):
         """(loss, loss_normalized), each of shape (1,) like the reference's."""
         self._sync_params()
-        params = list(self.model.parameters())
+        params = self.params
         if save_graph and torch.is_grad_enabled() and any(p.requires_grad for p in params):
             self.loss, self.loss_normalized = _FusedLoss.apply(self, *params)
         else:
