@@ -110,7 +110,7 @@ def test_unregistered_coefficient_gets_gradient():
     before = float(lam1.detach())
     model.train(T.Optimizer('Adam', {'lr': 1e-3}), 4)
     assert float(lam1.detach()) == before
-    assert float(net.lam2) != float(g['weights'][1])
+    assert float(net.lam2.detach()) != float(g["weights"][1])
 
 
 @pytest.mark.gpu

@@ -165,3 +165,23 @@ def test_device_parameter_order_and_optimizer_order():
     net.register_parameter('stray', torch.nn.Parameter(torch.zeros(3)))
     with pytest.raises(NotImplementedError):
         device_parameters(net, ir.coeff_params)
+
+
+def test_parameter_registr_and_inverse_task(capsys):
+    """parameter_registr registers one-element float32 parameters and puts them in the dict;
+    InverseTask prints name=value of those parameters on its epochs."""
+    import types
+    import torch_de_solver_gb300 as T
+    net = cases.mlp([2, 8, 1], 0)
+    params = {'lam1': 2.0, 'lam2': 0.2}
+    T.parameter_registr(net, params)
+    assert params['lam1'] is net.lam1 and params['lam2'] is net.lam2
+    assert net.lam1.dtype == torch.float32 and net.lam1.shape == (1,) and net.lam1.requires_grad
+    cb = T.InverseTask(parameters=params, info_string_every=2)
+    cb.set_model(types.SimpleNamespace(t=3, net=net))
+    cb.on_epoch_end()
+    assert capsys.readouterr().out == ''
+    cb.model.t = 4
+    cb.on_epoch_end()
+    out = capsys.readouterr().out
+    assert out.startswith('lam1=2.0 lam2=0.2') and out.strip().endswith(str(net.lam2.item()))

@@ -65,3 +65,23 @@ class CallbackList(Callback):
     def on_train_end(self, logs=None):
         for cb in self.callbacks:
             cb.on_train_end(logs or {})
+
+
+class InverseTask(Callback):
+    """Prints the trainable equation coefficients every `info_string_every` epochs
+    (tedeous/callbacks/inverse_task.py:8-38): `name=value` for each network parameter named in
+    `parameters`."""
+
+    def __init__(self, parameters: dict, info_string_every=None):
+        super().__init__()
+        self.parameters = parameters
+        self.info_string_every = info_string_every
+
+    def str_param(self):
+        if self.info_string_every is not None and self.model.t % self.info_string_every == 0:
+            names = set(self.parameters)
+            print(''.join(f'{name}={p.item()} ' for name, p in self.model.net.named_parameters()
+                          if name in names))
+
+    def on_epoch_end(self, logs=None):
+        self.str_param()

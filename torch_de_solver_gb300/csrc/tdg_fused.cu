@@ -187,6 +187,67 @@ __device__ void gemm_dw(const float* __restrict__ Gz, const float* __restrict__ 
 
 // In place: Z (pre-activations of every stream) -> H (tanh jet). Streams of a site are processed
 // from the highest order down so that lower-order Z values are still intact when read.
+// d loss / d theta_k summed over each warp's points into cred[warp][k]. The point's program is
+// evaluated again (outputs, seeds, then seed * scale * product per trainable term; scale = the
+// term's coefficient in the plan, `gterms`), so the kernel's own program loop stays as it is for
+// problems without trainable coefficients. Called by every thread of the CTA.
+__device__ __noinline__ void coeff_grad_warps(const DevGroup& G, const DevTerm* __restrict__ gterms,
+                                              const float* const* arrays, const float* ybuf, int T,
+                                              int nvalid, int row0, int n_coeff, float* cred) {
+  const int p = threadIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool valid = p < T && p < nvalid;
+  const int n_out = G.n_outputs;
+  float seed[MAX_OUT];
+#pragma unroll
+  for (int o = 0; o < MAX_OUT; ++o) seed[o] = 0.f;
+  if (valid) {
+    float outv[MAX_OUT];
+#pragma unroll
+    for (int o = 0; o < MAX_OUT; ++o) outv[o] = 0.f;
+    for (int t = 0; t < G.n_terms; ++t) {
+      const DevTerm& tm = G.terms[t];
+      const float c = tm.coeff_array >= 0 ? arrays[tm.coeff_array][row0 + p] : tm.coeff;
+      float prod = 1.f;
+      for (int f = 0; f < tm.n_factors; ++f) {
+        const DevFactor& fc = G.factors[tm.factor_first + f];
+        float F = 0.f;
+        for (int u = 0; u < fc.n_parts; ++u) {
+          const DevPart& pt = G.parts[fc.part_first + u];
+          F = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, F);
+        }
+        prod *= pow_f(F, fc.power);
+      }
+      outv[tm.output] += c * prod;
+    }
+    for (int o = 0; o < n_out; ++o) {
+      const float tgt = G.target_array >= 0 ? arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
+      seed[o] = (outv[o] - tgt) * G.seed_scale[o];
+    }
+  }
+  for (int k = 0; k < n_coeff; ++k) {
+    float v = 0.f;
+    if (valid)
+      for (int t = 0; t < G.n_terms; ++t) {
+        const DevTerm& tm = G.terms[t];
+        if (tm.coeff_param != k) continue;
+        float prod = 1.f;
+        for (int f = 0; f < tm.n_factors; ++f) {
+          const DevFactor& fc = G.factors[tm.factor_first + f];
+          float F = 0.f;
+          for (int u = 0; u < fc.n_parts; ++u) {
+            const DevPart& pt = G.parts[fc.part_first + u];
+            F = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, F);
+          }
+          prod *= pow_f(F, fc.power);
+        }
+        v += seed[tm.output] * gterms[t].coeff * prod;
+      }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) cred[warp * TDG_MAX_COEFF + k] = v;
+  }
+}
+
 __device__ void jet_forward(float* __restrict__ buf, const DevGroup& G, int N) {
   const int T = G.T;
   for (int e = threadIdx.x; e < T * N; e += NT) {
@@ -311,6 +372,13 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       for (int e = tid; e < (int)(sizeof(DevGroup) / 16); e += NT) dst[e] = src[e];
       cur_group = tile.group;
       __syncthreads();
+      if (A.n_coeff > 0) {   // trainable coefficients: the shared copy carries scale * theta
+        const float* theta = A.params + (int64_t)Gs->problem * A.n_params + A.coeff_off;
+        for (int t = tid; t < Gs->n_terms; t += NT)
+          if (Gs->terms[t].coeff_param >= 0)
+            Gs->terms[t].coeff = A.groups[tile.group].terms[t].coeff * theta[Gs->terms[t].coeff_param];
+        __syncthreads();
+      }
     }
     const DevGroup& G = *Gs;
     const int T = G.T, S = G.S, R = T * S;
@@ -399,9 +467,6 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     float err2[MAX_OUT];
 #pragma unroll
     for (int o = 0; o < MAX_OUT; ++o) err2[o] = 0.f;
-    float gc[TDG_MAX_COEFF];   // this point's d loss / d trainable coefficient
-#pragma unroll
-    for (int k = 0; k < TDG_MAX_COEFF; ++k) gc[k] = 0.f;
     if (tid < T) {
       const int p = tid;
       const bool valid = p < nvalid;
@@ -410,8 +475,7 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       for (int o = 0; o < MAX_OUT; ++o) outv[o] = 0.f;
       for (int t = 0; t < G.n_terms; ++t) {
         const DevTerm& tm = G.terms[t];
-        const float c = tm.coeff_param >= 0 ? tm.coeff * __ldg(&prm[A.coeff_off + tm.coeff_param])
-                        : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+        const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
         float prod = 1.f;
         for (int f = 0; f < tm.n_factors; ++f) {
           const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -439,10 +503,9 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       if (A.do_grad) {
         for (int t = 0; t < G.n_terms; ++t) {
           const DevTerm& tm = G.terms[t];
-          const float c = tm.coeff_param >= 0 ? tm.coeff * __ldg(&prm[A.coeff_off + tm.coeff_param])
-                          : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+          const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
           const float dt = seed[tm.output] * c;
-          if (dt == 0.f && tm.coeff_param < 0) continue;
+          if (dt == 0.f) continue;
           float F[MAX_TERM_FACTORS];
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -452,14 +515,6 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
               v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
             }
             F[f] = v;
-          }
-          if (tm.coeff_param >= 0) {   // d loss / d coefficient: seed * scale * product
-            float prod = 1.f;
-            for (int f = 0; f < tm.n_factors; ++f) prod *= pow_f(F[f], G.factors[tm.factor_first + f].power);
-#pragma unroll
-            for (int k = 0; k < TDG_MAX_COEFF; ++k)
-              if (k == tm.coeff_param) gc[k] += seed[tm.output] * tm.coeff * prod;
-            if (dt == 0.f) continue;
           }
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -489,16 +544,8 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
         for (int w = 0; w < NT / 32; ++w) s += wred[w * MAX_OUT + tid];
         slot_acc[G.slot_first + tid] += s;
       }
-      if (A.do_grad && A.n_coeff > 0) {   // coefficient gradients: warp shuffle, warps in order below
-#pragma unroll
-        for (int k = 0; k < TDG_MAX_COEFF; ++k) {
-          if (k >= A.n_coeff) break;
-          float v = gc[k];
-#pragma unroll
-          for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-          if (lane == 0) cred[warp * TDG_MAX_COEFF + k] = v;
-        }
-      }
+      if (A.do_grad && A.n_coeff > 0)   // coefficient gradients per warp; warps in order below
+        coeff_grad_warps(G, A.groups[tile.group].terms, A.arrays, ybuf, T, nvalid, row0, A.n_coeff, cred);
     }
     if (!A.do_grad) continue;
     __syncthreads();

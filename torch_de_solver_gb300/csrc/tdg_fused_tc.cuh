@@ -58,6 +58,44 @@ __device__ __forceinline__ float dpowf_(float x, float p) {
   return p * powf(x, p - 1.f);
 }
 
+// d loss / d theta_k of one tile: per (point, trainable term) seed * scale * product of the factors
+// (scale = the term's own coefficient in the plan, `gterms`), into the dead term-value rows `tv`,
+// then one thread per coefficient sums its terms and points in a fixed order and adds the sum to
+// the tile's gradient segment. Out of line: the kernels without trainable coefficients keep their
+// term loops unchanged. Called by every thread of the CTA.
+__device__ __noinline__ void coeff_grad_tile(const DevGroup& G, const DevTerm* __restrict__ gterms,
+                                             const float* ybuf, const float* seedv, float* tv, int T,
+                                             float* cgrad, int n_coeff) {
+  const int nt = G.n_terms;
+  for (int e = threadIdx.x; e < T * nt; e += blockDim.x) {
+    const int p = e % T, t = e / T;
+    const DevTerm& tm = G.terms[t];
+    if (tm.coeff_param < 0) continue;
+    float prod = 1.f;
+    for (int f = 0; f < tm.n_factors; ++f) {
+      const DevFactor& fc = G.factors[tm.factor_first + f];
+      float v = 0.f;
+      for (int u = 0; u < fc.n_parts; ++u) {
+        const DevPart& pt = G.parts[fc.part_first + u];
+        v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
+      }
+      prod *= powf_(v, fc.power);
+    }
+    tv[t * RMAX + p] = seedv[tm.output * RMAX + p] * gterms[t].coeff * prod;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n_coeff; k += blockDim.x) {
+    float sum = 0.f;
+    bool used = false;
+    for (int t = 0; t < nt; ++t)
+      if (G.terms[t].coeff_param == k) {
+        used = true;
+        for (int p = 0; p < T; ++p) sum += tv[t * RMAX + p];
+      }
+    if (used) red_add1(&cgrad[k], sum);
+  }
+}
+
 __device__ __forceinline__ float4 f4mul(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
 __device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 __device__ __forceinline__ float4 f4scale(float4 a, float c) { return make_float4(a.x * c, a.y * c, a.z * c, a.w * c); }
@@ -772,6 +810,12 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         for (int k = tid; k < A.n_coeff; k += NTC) pbuf[PB_CF + k] = pp[A.coeff_off + k];
       }
       __syncthreads();
+      if (A.n_coeff > 0) {   // trainable coefficients: the shared copy carries scale * theta
+        for (int t = tid; t < Gs->n_terms; t += NTC)
+          if (Gs->terms[t].coeff_param >= 0)
+            Gs->terms[t].coeff = A.groups[tile.group].terms[t].coeff * pbuf[PB_CF + Gs->terms[t].coeff_param];
+        __syncthreads();
+      }
     }
     const DevGroup& G = *Gs;
     const int T = G.T, S = G.S, R = T * S;
@@ -958,8 +1002,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const int p = e % T, t = e / T;
         const DevTerm& tm = G.terms[t];
         const bool valid = p < nvalid;
-        const float c = tm.coeff_param >= 0 ? tm.coeff * pbuf[PB_CF + tm.coeff_param]
-                        : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+        const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
         float prod = 1.f;
         for (int f = 0; f < tm.n_factors; ++f) {
           const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -998,11 +1041,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           const int p = e % T, t = e / T;
           const DevTerm& tm = G.terms[t];
           const bool valid = p < nvalid;
-          const float c = tm.coeff_param >= 0 ? tm.coeff * pbuf[PB_CF + tm.coeff_param]
-                          : tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
-          const float sd = seedv[tm.output * RMAX + p];
-          const float dt = sd * c;
-          if (dt == 0.f && tm.coeff_param < 0) continue;
+          const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
+          const float dt = seedv[tm.output * RMAX + p] * c;
+          if (dt == 0.f) continue;
           float F[MAX_TERM_FACTORS];
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -1012,12 +1053,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
               v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
             }
             F[f] = v;
-          }
-          if (tm.coeff_param >= 0) {   // d loss / d coefficient: seed * scale * product (term values are dead)
-            float prod = 1.f;
-            for (int f = 0; f < tm.n_factors; ++f) prod *= powf_(F[f], G.factors[tm.factor_first + f].power);
-            tv[t * RMAX + p] = sd * tm.coeff * prod;
-            if (dt == 0.f) continue;
           }
           for (int f = 0; f < tm.n_factors; ++f) {
             const DevFactor& fc = G.factors[tm.factor_first + f];
@@ -1030,20 +1065,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             }
           }
         }
-        if (A.n_coeff > 0) {   // one thread per coefficient: its terms and points in order
-          __syncthreads();
-          float* cgrad = A.partial + (int64_t)tile.seg * A.part_stride + A.coeff_off;
-          for (int k = tid; k < A.n_coeff; k += NTC) {
-            float sum = 0.f;
-            bool used = false;
-            for (int t = 0; t < nt; ++t)
-              if (G.terms[t].coeff_param == k) {
-                used = true;
-                for (int p = 0; p < T; ++p) sum += tv[t * RMAX + p];
-              }
-            if (used) red_add1(&cgrad[k], sum);
-          }
-        }
+        if (A.n_coeff > 0)
+          coeff_grad_tile(G, A.groups[tile.group].terms, ybuf, seedv, tv, T,
+                          A.partial + (int64_t)tile.seg * A.part_stride + A.coeff_off, A.n_coeff);
       }
     }
     if (!A.do_grad) continue;

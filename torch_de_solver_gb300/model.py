@@ -21,6 +21,15 @@ from .optimizer import FusedAdam, Optimizer
 from .solution import Solution
 
 
+def parameter_registr(model: torch.nn.Module, parameters: dict) -> None:
+    """Registers each initial value in `parameters` as a one-element float32 nn.Parameter of
+    `model` and replaces the dict entry by it, so that an equation term can use it as a trainable
+    coefficient (tedeous/models.py:183-196)."""
+    for key, value in parameters.items():
+        parameters[key] = torch.nn.Parameter(torch.tensor([value], requires_grad=True).float())
+        model.register_parameter(key, parameters[key])
+
+
 class Model:
     def __init__(self, net: torch.nn.Module, domain: Domain, equation: Equation,
                  conditions: Conditions, batch_size: int = None):
