@@ -25,6 +25,11 @@
  *   tdg_dot_f64
  *       the dot products of the L-BFGS two-loop recursion (torch.optim.LBFGS selected at
  *       tedeous/optimizers/optimizer.py:50-51), computed in FP64.
+ *   tdg_causal_weights
+ *       the time weights of the causal loss, Losses._causal_loss: tedeous/losses.py:137-182.
+ *   tdg_gather_rows
+ *       the mini-batch of collocation points drawn by the DataLoader of Operator:
+ *       tedeous/eval.py:119-144 (_pde_compute :172-183).
  *
  * Conventions: every pointer passed to a compute entry point is a device pointer owned by the
  * caller; nothing here frees caller memory. Calls are asynchronous on the given stream and never
@@ -42,7 +47,7 @@
 extern "C" {
 #endif
 
-#define TDG_ABI_VERSION 2
+#define TDG_ABI_VERSION 3
 
 #define TDG_MAX_LAYERS 12      /* Linear layers of the MLP */
 #define TDG_MAX_DIN 4          /* input coordinates per point */
@@ -131,7 +136,9 @@ typedef struct {
 
 /* a group of rows sharing one site/stream layout and one operator program. Output o of row i is
  * compared with target[i * n_outputs + o] (0 when target_array < 0) and its squared error is
- * added to loss slot slot_first + o. */
+ * added to loss slot slot_first + o. row_weight_array >= 0 names an array of n_rows floats w_i that
+ * multiply row i's squared errors and, held constant, its gradient (the causal loss's time
+ * weights, tedeous/losses.py:137-182; tdg_causal_weights computes them). */
 typedef struct {
   int32_t problem;           /* which parameter set (0 for a single solve) */
   int32_t n_rows;
@@ -140,6 +147,7 @@ typedef struct {
   int32_t n_outputs;
   int32_t slot_first;
   int32_t target_array;
+  int32_t row_weight_array;  /* -1: every row weighs 1 */
   int64_t output_offset;     /* where rows' outputs go in the optional outputs buffer; -1: none */
 } tdg_group_desc;
 
@@ -241,6 +249,18 @@ tdg_status tdg_dot_f64(const float* a, const float* b, int64_t n, double* out,
 #define TDG_DOT_NOALLOC_MAX_N (TDG_DOT_NOALLOC_MAX_BLOCKS * TDG_DOT_NOALLOC_CHUNK)
 tdg_status tdg_dot_f64_noalloc(const float* a, const float* b, int64_t n, double* out,
                                tdg_stream_t stream);
+
+/* Causal-loss weights of a residual field op[n_rows][n_eq] (row-major floats) whose rows form n_t
+ * time slices of rest = n_rows / n_t adjacent rows: with res_i = sum_e op[i][e]^2 and row
+ * i = s * rest + k, w[i] = exp(-tol * sum over s' < s of res[s' * rest + k]), the sum in FP64
+ * (tedeous/losses.py:160-168). n_rows must be a multiple of n_t (TDG_ERR_SHAPE otherwise). */
+tdg_status tdg_causal_weights(const float* op, int64_t n_rows, int32_t n_eq, int64_t n_t, float tol,
+                              float* w, tdg_stream_t stream);
+
+/* dst[r][c] = src[index[r]][c] for r < n and c < row_len (device arrays; index is int64). An
+ * index outside [0, n_src) gives a zero row. */
+tdg_status tdg_gather_rows(const float* src, int64_t n_src, const int64_t* index, int64_t n,
+                           int32_t row_len, float* dst, tdg_stream_t stream);
 
 #ifdef __cplusplus
 }

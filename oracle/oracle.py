@@ -277,7 +277,7 @@ class Problem:
     (tedeous/solution.py:23-168)."""
 
     def __init__(self, domain, conditions, equation, mode, lambda_operator, lambda_bound,
-                 h=0.001, inner_order='1', boundary_order='2'):
+                 h=0.001, inner_order='1', boundary_order='2', tol=0, batch_size=None):
         if mode not in ('NN', 'autograd'):
             raise NotImplementedError(mode)
         self.mode = mode
@@ -305,6 +305,24 @@ class Problem:
         else:
             self.points = self.grid
             self.prep = [self._prep_ag(e) for e in self.equations]
+        # causal loss: time slices = distinct values of the first coordinate of the residual
+        # points (tedeous/solution.py:49-56)
+        self.tol = tol
+        self.n_t = len((self.grid_dict['central'] if mode == 'NN' else self.grid)[:, 0].unique())
+        # mini-batches of the collocation points (tedeous/model.py:107-109, tedeous/eval.py:119-144):
+        # a shuffling DataLoader with an unseeded torch.Generator over the (type-sorted) grid; each
+        # residual evaluation takes the current batch and moves on, a new pass starts after the last
+        if batch_size is not None and len(self.grid) < batch_size:
+            batch_size = None
+        self.batch_size = batch_size
+        if batch_size is not None:
+            from torch.utils.data import DataLoader
+            sorted_grid = torch.cat(list(self.grid_dict.values())) if mode == 'NN' else self.grid
+            self.loader = DataLoader(sorted_grid, batch_size=batch_size, shuffle=True,
+                                     generator=torch.Generator())
+            self.n_batches = len(self.loader)
+            self._batches = iter(self.loader)
+            self._batch = next(self._batches)
 
     # coefficient resolution (tedeous/input_preprocessing.py:266-295, :433-458)
     def _coeff_nn(self, coeff, pts):
@@ -401,10 +419,18 @@ class Problem:
 
     # residual and boundaries -------------------------------------------------------------
     def residual(self, net):
+        pts = self.grid
+        if self.batch_size is not None:   # 'NN' terms ignore the batch (tedeous/derivative.py:30-58)
+            pts = self._batch
+            try:
+                self._batch = next(self._batches)
+            except StopIteration:
+                self._batches = iter(self.loader)
+                self._batch = next(self._batches)
         if self.mode == 'NN':
             cols = [self._apply_nn(net, p).reshape(-1, 1) for p in self.prep]
         else:
-            pts = self.grid.clone()
+            pts = pts.clone()
             cols = [self._apply_ag(net, p, pts).reshape(-1, 1) for p in self.prep]
         return cols[0] if len(cols) == 1 else torch.cat(cols, 1)
 
@@ -482,13 +508,40 @@ class Problem:
         dt = op.dtype
         lo = self._lambdas(op, self.lambda_operator).to(dt)
         lb = self._lambdas(bval, self.lambda_bound).to(dt)
-        op_mse = torch.mean(op ** 2, 0)
         b_mse = torch.mean((bval - true) ** 2, 0)
-        loss = op_mse @ lo.T + b_mse @ lb.T
-        with torch.no_grad():
-            lossn = op_mse @ torch.ones_like(lo).T + b_mse @ torch.ones_like(lb).T
+        if self.tol != 0:
+            loss, lossn = self._causal(op, b_mse, lb)
+        else:
+            op_mse = torch.mean(op ** 2, 0)
+            loss = op_mse @ lo.T + b_mse @ lb.T
+            with torch.no_grad():
+                lossn = op_mse @ torch.ones_like(lo).T + b_mse @ torch.ones_like(lb).T
         return dict(op=op, bval=bval, true_bval=true, keys=keys, lengths=lens,
                     loss=loss, loss_normalized=lossn)
+
+
+    def _causal(self, op, b_mse, lb):
+        """Causal loss (tedeous/losses.py:137-182): per-point residual res = sum over equations of
+        op^2 in [n_t, -1] time-slice rows, each weighted by exp(-tol * sum of res over the earlier
+        slices of its column) held constant; lambda_operator is not applied. In mini-batch mode n_t
+        is the number of distinct values in the first residual column (tedeous/solution.py:54
+        applied to the operator); a reshape that does not fit makes every row its own slice."""
+        if self.batch_size is not None:
+            self.n_t = len(op[:, 0].unique())
+        res = torch.sum(op ** 2, dim=1)
+        try:
+            res = res.reshape(self.n_t, -1)
+        except RuntimeError:
+            self.n_t = op.shape[0]
+            res = res.reshape(self.n_t, -1)
+        m = torch.triu(torch.ones((self.n_t, self.n_t), dtype=res.dtype), diagonal=1).T
+        with torch.no_grad():
+            w = torch.exp(-self.tol * (m @ res))
+        loss_oper = torch.mean(w * res)
+        loss = loss_oper + b_mse @ lb.T
+        with torch.no_grad():
+            lossn = loss_oper + torch.ones_like(lb) @ b_mse
+        return loss, lossn
 
 
 def build_problem(builder, dtype='float32'):
@@ -513,19 +566,24 @@ def loss_and_grad(problem, net):
 
 
 def train_adam(problem, net, lr, epochs):
-    """Model.train with Adam: initial evaluate, then epochs-1 closure steps
-    (tedeous/model.py:154-193). Returns the losses seen by each step's closure."""
+    """Model.train with Adam: initial evaluate, then epochs-1 epochs of one closure step each, or
+    of n_batches steps in mini-batch mode (tedeous/model.py:154-193). Returns the loss of each
+    epoch's last closure."""
     opt = torch.optim.Adam(net.parameters(), lr=lr)
     problem.evaluate(net)
     seen = []
+    steps = 1 if problem.batch_size is None else problem.n_batches
     for _ in range(epochs - 1):
         opt.zero_grad()
+        last = []
 
         def closure():
             opt.zero_grad()
             r = problem.evaluate(net)
             r['loss'].backward()
-            seen.append(float(r['loss'].detach().reshape(-1)[0]))
+            last.append(float(r['loss'].detach().reshape(-1)[0]))
             return r['loss']
-        opt.step(closure)
+        for _ in range(steps):
+            opt.step(closure)
+        seen.append(last[-1])
     return seen

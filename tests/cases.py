@@ -282,11 +282,49 @@ def inverse_burgers_ag(api, n=20, seed=6, dtype='float32', n_data=200, mode='aut
     return domain, bnd, eq, net, kw
 
 
+def allen_cahn_ag(api, n=20, seed=7, dtype='float32', tol=10.0, batch_size=None,
+                  widths=(2, 32, 32, 32, 1)):
+    """Allen-Cahn u_t - 1e-4 u_xx + 5u^3 - 5u = 0 with time as the first variable, periodic u and
+    u_x in x, the causal loss (tol) and optionally mini-batches of the collocation points (the setup
+    of examples/examples_allen_cahn/example_Allen_Cahn.py:20-104 and
+    example_Allen_Cahn_batches.py:102-104, with a plain tanh MLP instead of its Fourier features)."""
+    domain = api.Domain()
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    domain.variable('x', [-1, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [-1, 1], 't': 0}, value=lambda g: g[:, 1] ** 2 * torch.cos(np.pi * g[:, 1]))
+    bnd.periodic([{'x': -1, 't': [0, 1]}, {'x': 1, 't': [0, 1]}])
+    bnd.periodic([{'x': -1, 't': [0, 1]}, {'x': 1, 't': [0, 1]}],
+                 operator={'du/dx': {'coeff': 1, 'du/dx': [1], 'pow': 1, 'var': 0}})
+    eq = api.Equation()
+    eq.add({'1*du/dt**1': {'coeff': 1, 'du/dt': [0], 'pow': 1, 'var': 0},
+            '-0.0001*d2u/dx2**1': {'coeff': -0.0001, 'd2u/dx2': [1, 1], 'pow': 1, 'var': 0},
+            '+5u**3': {'coeff': 5, 'u': [None], 'pow': 3, 'var': 0},
+            '-5u**1': {'coeff': -5, 'u': [None], 'pow': 1, 'var': 0}})
+    net = mlp(list(widths), seed, getattr(torch, dtype))
+    kw = dict(mode='autograd', lambda_operator=1, lambda_bound=100, tol=tol)
+    if batch_size is not None:
+        kw['batch_size'] = batch_size
+    return domain, bnd, eq, net, kw
+
+
+def heat_causal_nn(api, n=12, dtype='float32', tol=1.0):
+    """The 'NN' heat problem with the causal loss (the first variable, x, plays time)."""
+    domain, bnd, eq, net, kw = heat_nn(api, n=n, dtype=dtype)
+    return domain, bnd, eq, net, dict(kw, tol=tol)
+
+
 COVERAGE_CASES = {
     'neumann_ag': lambda api, dtype='float32': neumann_ag(api, dtype=dtype),
     'robin_data_ag': lambda api, dtype='float32': robin_data_ag(api, dtype=dtype),
     'neumann_nn': lambda api, dtype='float32': neumann_nn(api, dtype=dtype),
     'inverse_burgers_ag': lambda api, dtype='float32': inverse_burgers_ag(api, dtype=dtype),
+    'allen_cahn_causal_ag': lambda api, dtype='float32': allen_cahn_ag(api, dtype=dtype),
+    'allen_cahn_batch_ag': lambda api, dtype='float32': allen_cahn_ag(api, dtype=dtype, tol=0,
+                                                                      batch_size=64),
+    'allen_cahn_batch_causal_ag': lambda api, dtype='float32': allen_cahn_ag(api, dtype=dtype,
+                                                                             batch_size=64),
+    'heat_causal_nn': lambda api, dtype='float32': heat_causal_nn(api, dtype=dtype),
 }
 GOLDEN_CASES.update(COVERAGE_CASES)
 

@@ -9,8 +9,11 @@ For each case in tests/cases.py GOLDEN_CASES this writes tests/golden/<case>.npz
   lossn32/64   loss_normalized of the same evaluate() call
   grad32/64    the flattened parameter gradient after loss.backward()
   op64         the first rows of the residual field (fp64) and op_sumsq64 = sum(op^2) per column
+               (mini-batch cases: the residual of the first batch, which the reference keeps as
+               save_op)
   bval64, true_bval64   boundary value matrices (fp64, padded per the reference)
   curve32      loss values seen by the closure over 5 Adam(lr=1e-3) steps of Model.train(6)
+               (mini-batch cases: the last closure loss of each of the 5 epochs, n_batches steps each)
   final32      parameters after those 5 steps
 The reference needs one stub: SALib (imported by tedeous/callbacks/adaptive_lambda.py:4) is
 absent, so an empty module is installed in sys.modules before the import.
@@ -51,16 +54,26 @@ def flat(tensors):
 def run_case(api, builder, dtype):
     domain, bnd, eq, net, kw = builder(api, dtype=dtype)
     w0 = flat(net.parameters()).astype(np.float32)
-    m = api.Model(net, domain, eq, bnd)
-    mode = kw.pop('mode')
-    m.compile(mode, **kw)
-    s = m.solution_cls
-    loss, lossn = s.evaluate()
-    loss.backward()
+    # The reference's causal loss makes its normalised boundary weights in torch's default dtype
+    # (tedeous/losses.py:176-181 through lambda_prepare), so its FP64 run needs float64 as the
+    # default dtype while it compiles and evaluates (after the network is built, so that the
+    # seeded initial weights stay the FP32 run's).
+    old_default = torch.get_default_dtype()
+    if dtype == 'float64' and kw.get('tol'):
+        torch.set_default_dtype(torch.float64)
+    try:
+        m = api.Model(net, domain, eq, bnd, batch_size=kw.pop('batch_size', None))
+        mode = kw.pop('mode')
+        m.compile(mode, **kw)
+        s = m.solution_cls
+        loss, lossn = s.evaluate()
+        loss.backward()
+    finally:
+        torch.set_default_dtype(old_default)
     grad = flat(p.grad for p in m.solution_cls.model.parameters())
     return dict(w0=w0, loss=float(loss.detach().reshape(-1)[0]),
                 lossn=float(lossn.detach().reshape(-1)[0]), grad=grad,
-                op=s.op.detach().to(torch.float64).numpy(),
+                op=(s.op if hasattr(s, 'op') else s.save_op).detach().to(torch.float64).numpy(),
                 bval=s.bval.detach().to(torch.float64).numpy(),
                 true_bval=s.true_bval.detach().to(torch.float64).numpy(),
                 bval_keys=list(s.bval_keys), bval_length=list(s.bval_length))
@@ -68,7 +81,7 @@ def run_case(api, builder, dtype):
 
 def run_curve(api, builder, steps=5):
     domain, bnd, eq, net, kw = builder(api, dtype='float32')
-    m = api.Model(net, domain, eq, bnd)
+    m = api.Model(net, domain, eq, bnd, batch_size=kw.pop('batch_size', None))
     mode = kw.pop('mode')
     m.compile(mode, **kw)
     seen = []

@@ -24,8 +24,8 @@ def build_model(api, name=None, builder=None, weights=None, precision='fp32', fo
     domain, bnd, eq, net, kw = builder(api, **case_kw) if case_kw else builder(api)
     if weights is not None:
         set_flat_weights(net, weights)
-    model = api.Model(net, domain, eq, bnd)
     kw = dict(kw)
+    model = api.Model(net, domain, eq, bnd, batch_size=kw.pop('batch_size', None))
     mode = kw.pop('mode')
     model.compile(mode, precision=precision, form=form, **kw)
     return model

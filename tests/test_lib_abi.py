@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.tdg_abi_version() == _lib.ABI_VERSION == 2
+    assert lib.tdg_abi_version() == _lib.ABI_VERSION == 3
 
 
 def test_struct_sizes_match_header():
@@ -43,3 +43,14 @@ def test_invalid_arguments_return_status():
     assert lib.tdg_adam_step(None, None, None, None, None, 0, None, None) == _lib.ERR_INVALID
     assert lib.tdg_dot_f64(None, None, 0, None, None) == _lib.ERR_INVALID
     assert lib.tdg_plan_destroy(None) == _lib.OK
+
+
+def test_causal_and_gather_reject_bad_shapes_without_a_gpu():
+    """The shape and null checks run on the host, before any launch."""
+    from torch_de_solver_gb300 import _lib
+    lib = _lib.load()
+    assert lib.tdg_causal_weights(None, 10, 1, 3, 1.0, None, None) == _lib.ERR_INVALID
+    assert lib.tdg_causal_weights(1, 10, 1, 3, 1.0, 1, None) == _lib.ERR_SHAPE   # 10 rows, 3 slices
+    assert b'time slices' in lib.tdg_last_error()
+    assert lib.tdg_gather_rows(None, 5, None, 0, 2, None, None) == _lib.OK         # nothing to do
+    assert lib.tdg_gather_rows(1, 5, 1, 4, 0, 1, None) == _lib.ERR_SHAPE

@@ -34,10 +34,12 @@ def test_lowering_shapes(name):
     mode = kw.pop('mode')
     ir = lower(d.build(mode), eq.equation_lst, bc.build(d.variable_dict), mode,
                kw['lambda_operator'], kw['lambda_bound'], kw.get('h', 0.001),
-               d_out=net[-1].out_features)
+               d_out=net[-1].out_features, tol=kw.get('tol', 0))
     res = ir.groups[ir.residual_group]
     g = np.load(f'tests/golden/{name}.npz')
-    assert res.n_rows == int(g['n_op'])
+    # mini-batch cases keep the first batch's residual in the fixture
+    assert min(res.n_rows, kw.get('batch_size', res.n_rows)) == int(g['n_op'])
+    assert (ir.causal is not None) == bool(kw.get('tol', 0))
     assert [ir.max_len] == [int(max(g['bval_length']))]
     assert ir.bc_types == [str(k) for k in g['bval_keys']]
     for grp in ir.groups:
@@ -185,3 +187,39 @@ def test_parameter_registr_and_inverse_task(capsys):
     cb.on_epoch_end()
     out = capsys.readouterr().out
     assert out.startswith('lam1=2.0 lam2=0.2') and out.strip().endswith(str(net.lam2.item()))
+
+
+def test_causal_time_slices_and_slots():
+    """The causal loss counts the distinct first coordinates of the residual points as time
+    slices (every point its own slice when they do not split evenly) and weighs each residual
+    row 1/N, lambda_operator not applied."""
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300.prepare import lower, residual_time_slices
+    g = torch.cartesian_prod(torch.linspace(0, 1, 5), torch.linspace(0, 1, 7))
+    assert residual_time_slices(g) == 5
+    assert residual_time_slices(g[:-1]) == 34
+    d, bc, eq, net, kw = cases.allen_cahn_ag(T, n=6)
+    ir = lower(d.build('autograd'), eq.equation_lst, bc.build(d.variable_dict), 'autograd',
+               3.0, 100, tol=kw['tol'])
+    res = ir.groups[ir.residual_group]
+    assert ir.causal == (10.0, 7)
+    assert ir.slots[res.slot_first][1:] == (1.0 / 49, 1.0 / 49)
+    assert res.row_weight is not None and ir.arrays[res.row_weight].numel() == 49
+
+
+def test_minibatch_order_equals_reference_loader():
+    """The product's batches (indices into the grid) select the same points, in the same order and
+    over several passes, as the reference's DataLoader over the points (restated by the oracle)."""
+    from torch_de_solver_gb300.solution import _Batches
+    prob, _ = O.build_problem(cases.GOLDEN_CASES['allen_cahn_batch_ag'], 'float32')
+    b = _Batches(prob.grid.shape[0], 64)
+    assert b.n_batches == prob.n_batches == 7
+    for _ in range(2 * b.n_batches + 3):
+        want = prob._batch
+        idx = b.take()
+        try:
+            prob._batch = next(prob._batches)
+        except StopIteration:
+            prob._batches = iter(prob.loader)
+            prob._batch = next(prob._batches)
+        assert torch.equal(prob.grid[idx], want)

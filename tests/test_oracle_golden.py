@@ -29,7 +29,9 @@ def test_oracle_matches_reference(name, dtype):
         assert r['keys'] == [str(k) for k in g['bval_keys']]
 
 
-@pytest.mark.parametrize('name', ['heat_nn', 'burgers_ag', 'kdv_ag', 'inverse_burgers_ag'])
+@pytest.mark.parametrize('name', ['heat_nn', 'burgers_ag', 'kdv_ag', 'inverse_burgers_ag',
+                                  'allen_cahn_causal_ag', 'allen_cahn_batch_ag',
+                                  'allen_cahn_batch_causal_ag', 'heat_causal_nn'])
 def test_oracle_training_curve(name):
     """Model.train(6) with Adam(lr=1e-3): five closure losses, then the final weights."""
     g = golden(name)

@@ -19,7 +19,7 @@ MAX_ORDER = 3
 MAX_STREAMS = 16
 MAX_SITES = 16
 MAX_COEFF = 16
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_SHAPE, ERR_CUDA, ERR_TIMEOUT, ERR_NOMEM = range(7)
 PREC = {'fp32': 0, 'tf32': 1, '3xtf32': 2, 'bf16': 3}
@@ -57,7 +57,7 @@ class TermDesc(ctypes.Structure):
 class GroupDesc(ctypes.Structure):
     _fields_ = [('problem', i32), ('n_rows', i32), ('site_first', i32), ('n_sites', i32),
                 ('term_first', i32), ('n_terms', i32), ('n_outputs', i32), ('slot_first', i32),
-                ('target_array', i32), ('output_offset', i64)]
+                ('target_array', i32), ('row_weight_array', i32), ('output_offset', i64)]
 
 
 class SlotDesc(ctypes.Structure):
@@ -105,6 +105,8 @@ SIGNATURES = {
     'tdg_adam_step': (i32, [vp, vp, vp, vp, vp, i64, ctypes.POINTER(AdamDesc), vp]),
     'tdg_dot_f64': (i32, [vp, vp, i64, vp, vp]),
     'tdg_dot_f64_noalloc': (i32, [vp, vp, i64, vp, vp]),
+    'tdg_causal_weights': (i32, [vp, i64, i32, i64, f32, vp, vp]),
+    'tdg_gather_rows': (i32, [vp, i64, vp, i64, i32, vp, vp]),
 }
 DOT_NOALLOC_MAX_N = 4096 * 16384
 

@@ -221,7 +221,8 @@ __device__ __noinline__ void coeff_grad_warps(const DevGroup& G, const DevTerm* 
     }
     for (int o = 0; o < n_out; ++o) {
       const float tgt = G.target_array >= 0 ? arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
-      seed[o] = (outv[o] - tgt) * G.seed_scale[o];
+      const float rw = G.row_weight_array >= 0 ? arrays[G.row_weight_array][row0 + p] : 1.f;
+      seed[o] = (outv[o] - tgt) * G.seed_scale[o] * rw;
     }
   }
   for (int k = 0; k < n_coeff; ++k) {
@@ -495,8 +496,9 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
         const float tgt = (G.target_array >= 0 && valid)
                               ? A.arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
         const float e = valid ? outv[o] - tgt : 0.f;
-        err2[o] = e * e;
-        seed[o] = e * G.seed_scale[o];   // dL/d(out) = 2 * weight * (out - target)
+        const float rw = (G.row_weight_array >= 0 && valid) ? A.arrays[G.row_weight_array][row0 + p] : 1.f;
+        err2[o] = e * e * rw;
+        seed[o] = e * G.seed_scale[o] * rw;   // dL/d(out) = 2 * weight * row weight * (out - target)
         if (A.outputs && G.out_offset >= 0 && valid)
           A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = outv[o];
       }

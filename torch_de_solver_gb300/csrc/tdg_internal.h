@@ -54,7 +54,7 @@ struct DevPart {
 struct alignas(16) DevGroup {
   int32_t n_rows, T, S, n_sites;
   int32_t n_outputs, n_terms, problem, slot_first;
-  int32_t target_array, pad0;
+  int32_t target_array, row_weight_array;   // row_weight_array: per-row loss weights (-1: none)
   int64_t out_offset;
   float seed_scale[MAX_OUT];              // 2 * loss weight of each output's slot
   int32_t site_points[MAX_SITES];
@@ -177,6 +177,10 @@ cudaError_t launch_reduce_loss(const double* slot_partial, int n_ctas, int n_slo
                                cudaStream_t s);
 cudaError_t launch_adam(float* p, const float* g, float* m, float* v, float* step, int64_t n,
                         const tdg_adam_desc& hp, cudaStream_t s);
+cudaError_t launch_causal_weights(const float* op, int64_t n_rows, int n_eq, int64_t n_t,
+                                  float tol, float* w, cudaStream_t s);
+cudaError_t launch_gather_rows(const float* src, int64_t n_src, const int64_t* index, int64_t n,
+                               int row_len, float* dst, cudaStream_t s);
 cudaError_t launch_dot_f64(const float* a, const float* b, int64_t n, double* out,
                            cudaStream_t s);
 

@@ -265,8 +265,9 @@ __global__ void plain_program(const DevGroup* __restrict__ G, const float* const
     for (int o = 0; o < n_out; ++o) {
       const float tgt = G->target_array >= 0 ? arrays[G->target_array][(int64_t)i * n_out + o] : 0.f;
       const float e = outv[o] - tgt;
-      atomicAdd(&red[o], (double)e * e);
-      seed[o] = e * G->seed_scale[o];
+      const float rw = G->row_weight_array >= 0 ? arrays[G->row_weight_array][i] : 1.f;
+      atomicAdd(&red[o], (double)e * e * (double)rw);
+      seed[o] = e * G->seed_scale[o] * rw;
       if (outputs && G->out_offset >= 0) outputs[G->out_offset + (int64_t)i * n_out + o] = outv[o];
     }
     if (!do_grad) continue;

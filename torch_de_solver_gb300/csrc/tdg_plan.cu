@@ -334,6 +334,9 @@ tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d
   if (g.target_array >= d.n_arrays) return fail(TDG_ERR_INVALID, "target array out of range");
   if (g.target_array >= 0 && d.array_len[g.target_array] < (int64_t)g.n_rows * g.n_outputs)
     return fail(TDG_ERR_SHAPE, "target array shorter than rows x outputs");
+  if (g.row_weight_array >= d.n_arrays) return fail(TDG_ERR_INVALID, "row weight array out of range");
+  if (g.row_weight_array >= 0 && d.array_len[g.row_weight_array] < g.n_rows)
+    return fail(TDG_ERR_SHAPE, "row weight array shorter than the group");
   if (g.slot_first < 0 || g.slot_first + g.n_outputs > d.n_slots) return fail(TDG_ERR_INVALID, "slot range out of bounds");
   for (int o = 0; o < g.n_outputs; ++o) {
     const tdg_slot_desc& sl = d.slots[g.slot_first + o];
@@ -349,6 +352,7 @@ tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d
   G.problem = g.problem;
   G.slot_first = g.slot_first;
   G.target_array = g.target_array;
+  G.row_weight_array = g.row_weight_array < 0 ? -1 : g.row_weight_array;
   G.out_offset = g.output_offset;
   S_out = S;
   return TDG_OK;
@@ -716,6 +720,27 @@ tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float
   cudaError_t e = launch_adam(params, grad, exp_avg, exp_avg_sq, step, n, *hp,
                               reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "adam launch");
+  return TDG_OK;
+}
+
+tdg_status tdg_causal_weights(const float* op, int64_t n_rows, int32_t n_eq, int64_t n_t, float tol,
+                              float* w, tdg_stream_t stream) {
+  if (!op || !w) return fail(TDG_ERR_INVALID, "null argument");
+  if (n_rows < 1 || n_eq < 1 || n_t < 1 || n_rows % n_t != 0)
+    return fail(TDG_ERR_SHAPE, "causal weights: %lld rows do not form %lld time slices", (long long)n_rows,
+                (long long)n_t);
+  cudaError_t e = launch_causal_weights(op, n_rows, n_eq, n_t, tol, w, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "causal weights launch");
+  return TDG_OK;
+}
+
+tdg_status tdg_gather_rows(const float* src, int64_t n_src, const int64_t* index, int64_t n, int32_t row_len,
+                           float* dst, tdg_stream_t stream) {
+  if (n < 0 || n_src < 0 || row_len < 1) return fail(TDG_ERR_SHAPE, "gather: bad sizes");
+  if (n == 0) return TDG_OK;
+  if (!src || !index || !dst) return fail(TDG_ERR_INVALID, "null argument");
+  cudaError_t e = launch_gather_rows(src, n_src, index, n, row_len, dst, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "gather launch");
   return TDG_OK;
 }
 

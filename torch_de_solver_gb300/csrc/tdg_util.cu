@@ -97,7 +97,59 @@ __global__ void dot_finish_kernel(const double* __restrict__ partial, int n, dou
   }
 }
 
+// one thread per column k of the [n_t][rest] time-slice layout: a running FP64 sum of the
+// squared residuals of the earlier slices (rows of one slice are adjacent, so a warp's loads of
+// one slice are coalesced)
+__global__ void causal_weights_kernel(const float* __restrict__ op, int64_t rest, int n_eq,
+                                      int64_t n_t, float tol, float* __restrict__ w) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < rest;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int64_t s = 0; s < n_t; ++s) {
+      const int64_t i = s * rest + k;
+      w[i] = expf(-tol * (float)acc);
+      double r = 0.0;
+      for (int e = 0; e < n_eq; ++e) {
+        const double v = op[i * n_eq + e];
+        r += v * v;
+      }
+      acc += r;
+    }
+  }
+}
+
+__global__ void gather_rows_kernel(const float* __restrict__ src, int64_t n_src,
+                                   const int64_t* __restrict__ index, int64_t n, int row_len,
+                                   float* __restrict__ dst) {
+  const int64_t total = n * row_len;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / row_len, c = e - r * row_len;
+    const int64_t j = index[r];
+    dst[e] = (j >= 0 && j < n_src) ? src[j * row_len + c] : 0.f;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_causal_weights(const float* op, int64_t n_rows, int n_eq, int64_t n_t,
+                                  float tol, float* w, cudaStream_t s) {
+  const int64_t rest = n_rows / n_t;
+  int64_t blocks = (rest + 127) / 128;
+  if (blocks > 1216) blocks = 1216;
+  causal_weights_kernel<<<(int)blocks, 128, 0, s>>>(op, rest, n_eq, n_t, tol, w);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(const float* src, int64_t n_src, const int64_t* index, int64_t n,
+                               int row_len, float* dst, cudaStream_t s) {
+  int64_t blocks = (n * row_len + 255) / 256;
+  if (blocks > 1216) blocks = 1216;
+  gather_rows_kernel<<<(int)blocks, 256, 0, s>>>(src, n_src, index, n, row_len, dst);
+  count_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
                                const int32_t* seg_list, int n_problems, int64_t n_params,

@@ -49,11 +49,6 @@ class Model:
         """Arguments as in tedeous/model.py:56-113, plus precision ('fp32') and form ('fused')."""
         if weak_form:
             raise NotImplementedError('weak-form losses are not implemented on the device path')
-        if tol:
-            raise NotImplementedError('the causal loss (tol > 0) is not implemented on the '
-                                      'device path')
-        if self.batch_size is not None:
-            raise NotImplementedError('mini-batch training is not implemented on the device path')
         self.mode = mode
         self.lambda_bound = lambda_bound
         self.lambda_operator = lambda_operator
@@ -61,9 +56,12 @@ class Model:
         self.weak_form = weak_form
         grid = self.domain.build(mode=mode, removed_domains=removed_domains)
         bconds = self.conditions.build(self.domain.variable_dict)
+        if self.batch_size is not None and len(grid) < self.batch_size:
+            self.batch_size = None
         self.solution_cls = Solution(grid, self.equation.equation_lst, bconds, self.net, mode,
                                      lambda_operator, lambda_bound, h=h, inner_order=inner_order,
-                                     boundary_order=boundary_order, precision=precision, form=form)
+                                     boundary_order=boundary_order, precision=precision, form=form,
+                                     tol=tol, batch_size=self.batch_size)
         self.net = self.solution_cls.model
         self._graph = None
 
@@ -81,7 +79,7 @@ class Model:
             self._graph.replay()
             return self._loss32[0:1]
         sol._sync_params()
-        sol.plan.loss_grad(sol.flat, sol._grad, sol._loss_buf, sol._outputs)
+        sol._launch(with_grad=True)
         opt.apply(sol._grad)
         if capture:
             self._loss32 = torch.empty(2, device=sol.device)
@@ -89,7 +87,7 @@ class Model:
             stream.wait_stream(torch.cuda.current_stream(sol.device))
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, stream=stream):
-                sol.plan.loss_grad(sol.flat, sol._grad, sol._loss_buf, sol._outputs)
+                sol._launch(with_grad=True)
                 self._loss32.copy_(sol._loss_buf)
                 opt.apply(sol._grad)
             self._graph = g
@@ -117,17 +115,20 @@ class Model:
                  and optimizer.cosine_scheduler_patience is None and not self.normalized_loss_stop)
         self._graph = None
         n_eager = 0
+        batches = self.solution_cls.batches
+        steps = 1 if batches is None else batches.n_batches   # tedeous/model.py:178-185
         while self.t < epochs and self.stop_training is False:
             cbs.on_epoch_begin()
             self.optimizer.zero_grad()
-            if fused:
-                loss = self._fused_step(capture=(n_eager == 2))
-                n_eager += 1
-                self.cur_loss = loss.clone() if cbs.callbacks else loss
-            else:
-                self.optimizer.step(closure)
-                if optimizer.gamma is not None and self.t % optimizer.decay_every == 0:
-                    optimizer.scheduler.step()
+            for _ in range(steps):
+                if fused:   # mini-batch steps change their inputs on the host: no graph
+                    loss = self._fused_step(capture=(n_eager == 2 and batches is None))
+                    n_eager += 1
+                    self.cur_loss = loss.clone() if cbs.callbacks else loss
+                else:
+                    self.optimizer.step(closure)
+                    if optimizer.gamma is not None and self.t % optimizer.decay_every == 0:
+                        optimizer.scheduler.step()
             cbs.on_epoch_end()
             self.t += 1
             if info_string_every is not None and self.t % info_string_every == 0:

@@ -142,6 +142,7 @@ class Group:
         self.sites = []
         self.terms = []               # (coeff float | array key, output, [(var, power, [(site, stream, w)])])
         self.target = None            # array key of n_rows x n_outputs floats, or None (zeros)
+        self.row_weight = None        # array key of n_rows per-row loss weights, or None (ones)
         self.out_key = None           # (type, position) for boundary values
 
 
@@ -172,6 +173,7 @@ class ProblemIR:
         self.bc_true = {}             # type -> concatenated true values (float32)
         self.max_len = 0
         self.n_residual_rows = 0
+        self.causal = None            # (tol, n_t) of the causal loss, or None
 
     def coeff_index(self, param):
         """Slot of a trainable coefficient (one per distinct nn.Parameter)."""
@@ -557,9 +559,21 @@ def _lambda_list(lam, n):
     return v
 
 
+def residual_time_slices(points):
+    """n_t of the causal loss: the number of distinct values of the first coordinate of the
+    residual points (tedeous/solution.py:49-56); when the points do not split into n_t equal
+    slices, every point is its own slice (the fallback of tedeous/losses.py:161-165)."""
+    n = points.shape[0]
+    n_t = len(torch.unique(points.reshape(n, -1)[:, 0]))
+    return n_t if n % n_t == 0 else n
+
+
 def lower(grid, operator, bconds, mode, lambda_operator, lambda_bound, h=0.001, inner_order='1',
-          boundary_order='2', d_out=1):
-    """Build the ProblemIR of one problem: residual group(s), boundary groups and loss slots."""
+          boundary_order='2', d_out=1, tol=0):
+    """Build the ProblemIR of one problem: residual group(s), boundary groups and loss slots.
+    tol != 0 selects the causal loss (tedeous/losses.py:137-182): the residual rows weigh 1/N
+    each, times a per-row weight array that tdg_causal_weights fills before each evaluation;
+    lambda_operator is not applied, as in the reference."""
     lw = Lowering(grid, operator, bconds, mode, lambda_operator, lambda_bound, h, inner_order,
                   boundary_order, d_out)
     ir = lw.ir
@@ -570,8 +584,14 @@ def lower(grid, operator, bconds, mode, lambda_operator, lambda_bound, h=0.001, 
     n_eq = res.n_outputs
     lam_op = _lambda_list(lambda_operator, n_eq)
     n = float(res.n_rows)
-    for e in range(n_eq):
-        ir.slots.append((0, lam_op[e] / n, 1.0 / n))
+    if tol:
+        for e in range(n_eq):
+            ir.slots.append((0, 1.0 / n, 1.0 / n))
+        res.row_weight = ir.add_array(torch.ones(res.n_rows))
+        ir.causal = (float(tol), residual_time_slices(ir.arrays[res.sites[0].points]))
+    else:
+        for e in range(n_eq):
+            ir.slots.append((0, lam_op[e] / n, 1.0 / n))
     lw.boundary({})
     lens = {t: sum(r for _, r in ir.bc_parts[t]) for t in ir.bc_types}
     ir.max_len = max(lens.values())

@@ -129,9 +129,10 @@ class DevicePlan:
                     else:
                         terms.append(_lib.TermDesc(f_first, len(fl), output, base + coeff, 0.0, -1))
                 tgt = -1 if g.target is None else base + g.target
+                rw = -1 if g.row_weight is None else base + g.row_weight
                 groups.append(_lib.GroupDesc(prob, g.n_rows, site_first, len(g.sites), term_first,
                                              len(g.terms), g.n_outputs, slot_base + g.slot_first,
-                                             tgt, out_off))
+                                             tgt, rw, out_off))
                 offs.append(out_off)
                 out_off += g.n_rows * g.n_outputs
             self.group_out.append(offs)
@@ -223,12 +224,54 @@ class _FusedLoss(torch.autograd.Function):
         return (None, *out)
 
 
+def _residual_row_arrays(ir):
+    """Array keys of the residual group that hold one entry (or row) per residual point: its site
+    points and per-row coefficients, in first-reference order."""
+    g = ir.groups[ir.residual_group]
+    keys = []
+    for k in [s.points for s in g.sites] + [c for c, _, _ in g.terms if isinstance(c, int)]:
+        if k not in keys:
+            keys.append(k)
+    return keys
+
+
+class _Batches:
+    """Mini-batches of the collocation points with the reference's order: a shuffling DataLoader
+    with an unseeded torch.Generator over the (type-sorted) grid; each residual evaluation takes
+    the current batch and moves on, and a new pass starts after the last batch
+    (tedeous/eval.py:119-144, _pde_compute :172-183). It draws indices, which select the same
+    rows that the reference's DataLoader over the points draws."""
+
+    def __init__(self, n, batch_size):
+        from torch.utils.data import DataLoader
+        self.loader = DataLoader(torch.arange(n), batch_size=batch_size, shuffle=True,
+                                 generator=torch.Generator())
+        self.n_batches = len(self.loader)
+        self._it = iter(self.loader)
+        self._next = next(self._it)
+
+    def take(self):
+        idx = self._next
+        try:
+            self._next = next(self._it)
+        except StopIteration:
+            self._it = iter(self.loader)
+            self._next = next(self._it)
+        return idx
+
+
 class Solution:
-    """Loss evaluation of one compiled problem (tedeous/solution.py:19-168)."""
+    """Loss evaluation of one compiled problem (tedeous/solution.py:19-168).
+
+    tol != 0 selects the causal loss: a forward-only launch writes the residual field, then
+    tdg_causal_weights turns it into per-row weights, then the loss and gradient launch applies
+    them. batch_size selects mini-batches of the collocation points: in 'autograd' mode each
+    evaluation gathers the batch's points (and per-point coefficients) with tdg_gather_rows into
+    a plan made for that batch size; 'NN' terms ignore the batch, as the reference's do."""
 
     def __init__(self, grid, operator, bconds, model, mode, lambda_operator, lambda_bound,
                  h=0.001, inner_order='1', boundary_order='2', precision='fp32', form='fused',
-                 device=None):
+                 device=None, tol=0, batch_size=None):
         if not torch.cuda.is_available():
             raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
         self.device = torch.device('cuda', torch.cuda.current_device()) if device is None \
@@ -237,16 +280,46 @@ class Solution:
         self.grid = grid
         self.lambda_operator, self.lambda_bound = lambda_operator, lambda_bound
         widths = mlp_widths(model)
-        self.ir = lower(grid, operator, bconds, mode, lambda_operator, lambda_bound, h,
-                        inner_order, boundary_order, d_out=widths[-1])
+        if batch_size is not None and mode == 'NN' and tol:
+            raise NotImplementedError("the causal loss with mini-batches in 'NN' mode (the "
+                                      "reference's time-slice count fails there)")
+        args = (operator, bconds, mode, lambda_operator, lambda_bound, h, inner_order,
+                boundary_order)
+        self.ir = lower(grid, *args, d_out=widths[-1], tol=tol)
         self.model = model.to(self.device)
         self.params = device_parameters(self.model, self.ir.coeff_params)
         self.flat = flatten_parameters(self.params, self.device)
         self._shapes = [(p.shape, p.numel()) for p in self.params]
-        self.plan = DevicePlan([self.ir], widths, self.device, precision, form)
+        self.batches = None if batch_size is None else _Batches(grid.shape[0], batch_size)
+        self._plans = {}
+        if self.batches is not None and mode == 'autograd':
+            # one plan per batch size (full batches and the last, shorter one), each lowered on
+            # placeholder rows that every evaluation overwrites by a gather from the full arrays
+            full = _residual_row_arrays(self.ir)
+            n_grid = grid.shape[0]
+            sizes = sorted({min(batch_size, n_grid - i) for i in range(0, n_grid, batch_size)},
+                           reverse=True)
+            self._row_src = {k: self.ir.arrays[k].to(self.device).reshape(-1)
+                             for k in full}
+            for n in sizes:
+                ir_b = lower(grid[:n], *args, d_out=widths[-1], tol=tol)
+                if len(ir_b.coeff_params) != len(self.ir.coeff_params):
+                    raise RuntimeError('batch lowering changed the trainable coefficients')
+                ir_b.coeff_params = self.ir.coeff_params
+                plan = DevicePlan([ir_b], widths, self.device, precision, form)
+                gathers = [(plan.arrays[kb], self._row_src[kf], self.ir.arrays[kf].numel() //
+                            grid.shape[0]) for kb, kf in zip(_residual_row_arrays(ir_b), full)]
+                self._plans[n] = (ir_b, plan, gathers)
+            self._idx = torch.zeros(batch_size, dtype=torch.int64, device=self.device)
+            self.ir, self.plan, _ = self._plans[sizes[0]]
+        else:
+            self.plan = DevicePlan([self.ir], widths, self.device, precision, form)
+            self._plans[self.ir.groups[self.ir.residual_group].n_rows] = (self.ir, self.plan, [])
         self._grad = torch.zeros(self.plan.n_params, device=self.device, dtype=torch.float32)
         self._loss_buf = torch.zeros(2, device=self.device, dtype=torch.float64)
-        self._outputs = torch.zeros(max(1, self.plan.n_outputs_total), device=self.device)
+        self._out_bufs = {n: torch.zeros(max(1, p.n_outputs_total), device=self.device)
+                          for n, (_, p, _) in self._plans.items()}
+        self._outputs = self._out_bufs[self.ir.groups[self.ir.residual_group].n_rows]
         self._clone_grad = True
         self.bval_keys = list(self.ir.bc_types)
         self.bval_length = [sum(r for _, r in self.ir.bc_parts[t]) for t in self.ir.bc_types]
@@ -266,7 +339,44 @@ class Solution:
             self.flat = flatten_parameters(self.params, self.device)
 
     # -- evaluation --------------------------------------------------------------------------
+    def _select_batch(self):
+        """'autograd' mini-batch mode: gather the next batch into the plan of its size."""
+        idx = self.batches.take()
+        n = idx.numel()
+        self.ir, self.plan, gathers = self._plans[n]
+        self._outputs = self._out_bufs[n]
+        self._idx[:n].copy_(idx, non_blocking=True)
+        lib = _lib.load()
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        n_src = self.grid.shape[0]
+        for dst, src, row_len in gathers:
+            _lib.check(lib.tdg_gather_rows(src.data_ptr(), n_src, self._idx.data_ptr(), n,
+                                           row_len, dst.data_ptr(), stream), 'tdg_gather_rows')
+
+    def _causal_weights(self):
+        """Forward-only launch for the residual field, then its causal row weights."""
+        ir = self.ir
+        tol, n_t = ir.causal
+        res = ir.groups[ir.residual_group]
+        self.plan.loss(self.flat, self._loss_buf, self._outputs)
+        off = self.plan.group_out[0][ir.residual_group]
+        if self.batches is not None:   # tedeous/solution.py:54 applied to the operator
+            op0 = self._outputs[off:off + res.n_rows * ir.n_eq].view(-1, ir.n_eq)[:, 0]
+            n_t = int(torch.unique(op0).numel())
+            if res.n_rows % n_t:
+                n_t = res.n_rows
+        w = self.plan.arrays[res.row_weight]
+        _lib.check(_lib.load().tdg_causal_weights(
+            self._outputs.data_ptr() + 4 * off, res.n_rows, ir.n_eq, n_t, tol, w.data_ptr(),
+            torch.cuda.current_stream(self.device).cuda_stream), 'tdg_causal_weights')
+
     def _launch(self, with_grad):
+        if self.batches is not None and self.mode == 'autograd':
+            self._select_batch()
+        elif self.batches is not None:
+            self.batches.take()
+        if self.ir.causal is not None:
+            self._causal_weights()
         if with_grad:
             self.plan.loss_grad(self.flat, self._grad, self._loss_buf, self._outputs)
         else:
