@@ -223,3 +223,18 @@ def test_minibatch_order_equals_reference_loader():
             prob._batches = iter(prob.loader)
             prob._batch = next(prob._batches)
         assert torch.equal(prob.grid[idx], want)
+
+
+def test_model_save_uses_the_reference_cache_file_names(tmp_path):
+    """Model._model_save writes cache_dir + '\\' + name + '.tar' with a CPU copy of the network,
+    the name the reference's cache lookup pattern cache_dir + '\\*.tar' finds."""
+    import glob
+    import torch_de_solver_gb300 as T
+    m = T.Model(cases.mlp([2, 8, 1], 0), None, None, None)
+    m._save_dir = str(tmp_path) + '/'
+    m._model_save(True, 'abc')
+    files = glob.glob(m._save_dir + '\\*.tar')
+    assert files == [m._save_dir + '\\abc.tar']
+    ck = torch.load(files[0], weights_only=False)
+    assert set(ck) == {'model', 'model_state_dict'}
+    assert torch.equal(ck['model'][0].weight, m.net[0].weight)

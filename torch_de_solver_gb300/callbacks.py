@@ -85,3 +85,202 @@ class InverseTask(Callback):
 
     def on_epoch_end(self, logs=None):
         self.str_param()
+
+
+def create_random_fn(eps):
+    """Adds (2 * randn - 1) * eps to the weight and bias of every Linear layer it is applied to
+    (tedeous/utils.py:14-30)."""
+    import torch
+
+    def randomize_params(m):
+        if isinstance(m, torch.nn.Linear) and m.bias is not None:
+            m.weight.data = m.weight.data + (2 * torch.randn(m.weight.size()) - 1).to(m.weight) * eps
+            m.bias.data = m.bias.data + (2 * torch.randn(m.bias.size()) - 1).to(m.bias) * eps
+    return randomize_params
+
+
+def remove_all_files(folder):
+    """Deletes every file and folder inside `folder` (tedeous/utils.py:100-114)."""
+    import os
+    import shutil
+    for filename in os.listdir(folder):
+        path = os.path.join(folder, filename)
+        try:
+            if os.path.isfile(path) or os.path.islink(path):
+                os.unlink(path)
+            elif os.path.isdir(path):
+                shutil.rmtree(path)
+        except Exception as e:
+            print('Failed to delete %s. Reason: %s' % (path, e))
+
+
+def count_output(model):
+    """out_features of the last layer that has one (tedeous/callbacks/cache.py:21-35)."""
+    for layer in reversed(list(model.modules())):
+        if hasattr(layer, 'out_features'):
+            return layer.out_features
+    return None
+
+
+class CachePreprocessing:
+    """Cache lookup and reuse for a compiled Model (tedeous/callbacks/cache.py:38-258). The lookup
+    evaluates every usable cached network on the current problem in one launch per network shape
+    (Solution.evaluate_many) instead of one evaluate per file, and keeps the reference's choice:
+    the first network with the smallest loss, in the order of the files found."""
+
+    def __init__(self, model):
+        self.solution_cls = model.solution_cls
+
+    @staticmethod
+    def _cache_files(files, nmodels=None):
+        import numpy as np
+        if nmodels is None:
+            return np.arange(len(files))
+        return np.random.choice(len(files), nmodels, replace=False)
+
+    @staticmethod
+    def _model_reform(init_model, model):
+        try:
+            model[0]
+        except Exception:
+            model = model.model
+        try:
+            init_model[0]
+        except Exception:
+            init_model = init_model.model
+        return init_model, model
+
+    def cache_lookup(self, cache_dir, nmodels=None, save_graph=False, cache_verbose=False):
+        """Best cached checkpoint {'model', 'model_state_dict'} by loss, or None. Files are found
+        with the reference's pattern cache_dir + '\\*.tar' (tedeous/callbacks/cache.py:117), which
+        matches the names Model saves under."""
+        import glob
+        import torch
+        from .solution import mlp_widths
+        files = glob.glob(cache_dir + '\\*.tar')
+        if cache_verbose:
+            print(f"The CACHE will be searched among the models in the folder {cache_dir}.")
+        if len(files) == 0:
+            return None
+        solver = self.solution_cls.model
+        candidates = []
+        for i in self._cache_files(files, nmodels):
+            file = files[i]
+            try:
+                checkpoint = torch.load(file, weights_only=False, map_location='cpu')
+            except Exception:
+                if cache_verbose:
+                    print('Error loading file {}'.format(file))
+                continue
+            model = checkpoint['model']
+            model.load_state_dict(checkpoint['model_state_dict'])
+            try:
+                solver_model, cache_model = self._model_reform(solver, model)
+            except Exception:
+                if cache_verbose:
+                    print('Error reforming file {}'.format(file))
+                continue
+            if cache_model[0].in_features != solver_model[0].in_features:
+                continue
+            try:
+                if count_output(model) != count_output(solver):
+                    continue
+                mlp_widths(model)
+            except Exception:   # includes networks the device path cannot evaluate
+                continue
+            candidates.append((i, model))
+        if not candidates:
+            return None
+        losses = self.solution_cls.evaluate_many([m for _, m in candidates])[:, 0].cpu()
+        best = int(torch.argmin(losses))   # the first of equal minima, as the reference's '<'
+        i, model = candidates[best]
+        if cache_verbose:
+            print('best_model_num={} , loss={}'.format(i, float(losses[best])))
+        return {'model': model, 'model_state_dict': model.state_dict()}
+
+    def scheme_interp(self, trained_model, cache_verbose=False):
+        """Fits the solver's network to the outputs of a cached network of another architecture
+        on the grid with Adam(lr=1e-3) until the mean squared difference is below 1e-5
+        (tedeous/callbacks/cache.py:183-219)."""
+        import torch
+        sol = self.solution_cls
+        grid = sol.grid.to(sol.device)
+        model = sol.model
+        trained_model = trained_model.to(sol.device)
+        optimizer = torch.optim.Adam(model.parameters(), lr=0.001)
+        loss = torch.mean(torch.square(trained_model(grid) - model(grid)))
+
+        def closure():
+            optimizer.zero_grad()
+            loss = torch.mean((trained_model(grid) - model(grid)) ** 2)
+            loss.backward()
+            return loss
+        t = 0
+        while loss > 1e-5 and t < 1e5:
+            optimizer.step(closure)
+            loss = torch.mean(torch.square(trained_model(grid) - model(grid)))
+            t += 1
+            if cache_verbose:
+                print('Interpolate from trained model t={}, loss={}'.format(t, loss))
+        sol._model_change(model)
+
+    def cache_retrain(self, cache_checkpoint, cache_verbose=False):
+        """Same architecture: continue from the cached network; otherwise fit the solver's network
+        to it (tedeous/callbacks/cache.py:221-258)."""
+        import torch
+        model = self.solution_cls.model
+        if cache_checkpoint is None:
+            return None
+        if str(cache_checkpoint['model']) == str(model) and isinstance(model, torch.nn.Sequential) \
+                and isinstance(model[0], torch.nn.Linear):
+            model = cache_checkpoint['model']
+            model.load_state_dict(cache_checkpoint['model_state_dict'])
+            model.train()
+            self.solution_cls._model_change(model)
+            if cache_verbose:
+                print('Using model from cache')
+        else:
+            cache_model = cache_checkpoint['model']
+            cache_model.load_state_dict(cache_checkpoint['model_state_dict'])
+            cache_model.eval()
+            self.scheme_interp(cache_model, cache_verbose=cache_verbose)
+
+
+class Cache(Callback):
+    """Starts training from the best cached network and points Model's save folder at the cache
+    (tedeous/callbacks/cache.py:261-400). 'mat' mode has no device path here."""
+
+    def __init__(self, nmodels=None, cache_dir='tedeous_cache', cache_verbose=False,
+                 cache_model=None, model_randomize_parameter=0, clear_cache=False):
+        import os
+        import tempfile
+        super().__init__()
+        self.nmodels = nmodels
+        self.cache_verbose = cache_verbose
+        self.cache_model = cache_model
+        self.model_randomize_parameter = model_randomize_parameter
+        if cache_dir == 'tedeous_cache':
+            folder = os.path.join(tempfile.gettempdir(), 'tedeous_cache/')
+            os.makedirs(folder, exist_ok=True)
+            self.cache_dir = folder
+        else:
+            self.cache_dir = cache_dir
+        if clear_cache:
+            remove_all_files(self.cache_dir)
+
+    def _cache_nn(self):
+        cache_preproc = CachePreprocessing(self.model)
+        r = create_random_fn(self.model_randomize_parameter)
+        checkpoint = cache_preproc.cache_lookup(cache_dir=self.cache_dir, nmodels=self.nmodels,
+                                                cache_verbose=self.cache_verbose)
+        cache_preproc.cache_retrain(checkpoint, cache_verbose=self.cache_verbose)
+        self.model.solution_cls.model.apply(r)
+
+    def cache(self):
+        if self.model.mode == 'mat':
+            raise NotImplementedError("'mat' mode is not implemented on the device path")
+        return self._cache_nn()
+
+    def on_train_begin(self, logs=None):
+        self.cache()
+        self.model._save_dir = self.cache_dir

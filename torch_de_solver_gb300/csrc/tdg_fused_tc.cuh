@@ -1026,7 +1026,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
                               ? A.arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
         const float err = valid ? out - tgt : 0.f;
         const float rw = (G.row_weight_array >= 0 && valid) ? A.arrays[G.row_weight_array][row0 + p] : 1.f;
-        e2[o * RMAX + p] = (double)err * (double)err * (double)rw;
+        e2[o * RMAX + p] = (double)err * (double)err * (double)rw;   // per-row loss weights (causal loss)
         seedv[o * RMAX + p] = err * G.seed_scale[o] * rw;
         if (A.outputs && G.out_offset >= 0 && valid)
           A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = out;

@@ -7,6 +7,7 @@ an initial evaluate(), then epochs - 1 optimizer steps, callbacks around every e
 (loss + gradient kernel, reductions, Adam update) is captured once in a CUDA graph and replayed.
 """
 
+import copy
 import datetime
 import os
 import tempfile
@@ -66,11 +67,16 @@ class Model:
         self._graph = None
 
     def _model_save(self, save_model: bool, model_name: str):
+        """Writes {'model', 'model_state_dict'} of a CPU copy of the network to the cache folder
+        under the reference's file name, cache_dir + '\\' + name + '.tar'
+        (tedeous/utils.py:172-199), which its cache lookup pattern '\\*.tar' finds."""
         if save_model:
             os.makedirs(self._save_dir, exist_ok=True)
             name = model_name or str(datetime.datetime.now().timestamp())
-            torch.save({'model': self.net, 'model_state_dict': self.net.state_dict()},
-                       os.path.join(self._save_dir, name + '.tar'))
+            net = copy.deepcopy(self.net).to('cpu')
+            torch.save({'model': net, 'model_state_dict': net.state_dict()},
+                       self._save_dir + '\\' + name + '.tar')
+            print(f'model is saved in cache dir: {self._save_dir}')
 
     def _fused_step(self, capture: bool):
         """loss+gradient, Adam; returns the (1,) loss seen before the update."""
@@ -103,6 +109,7 @@ class Model:
         self.stop_training = False
         cbs = CallbackList(callbacks=callbacks, model=self)
         cbs.on_train_begin()
+        self.solution_cls._sync_params()   # a callback may have swapped or re-seated the network
         self.net = self.solution_cls.model
         self.optimizer = optimizer.optimizer_choice(self.mode, self.net)
         closure = Closure(mixed_precision, self).get_closure(optimizer.optimizer)

@@ -41,15 +41,17 @@ def mlp_widths(net):
     return widths
 
 
-def device_parameters(net, coeff_params=()):
+def device_parameters(net, coeff_params=(), strict=True):
     """The parameters in the order of the device's flat buffer: every Linear layer's weight and
     bias in layer order, then the equation's trainable coefficients (ProblemIR.coeff_params).
-    Other parameters of `net` have no place on the device path."""
+    Other parameters of `net` have no place on the device path: strict raises for them, otherwise
+    they are left out (a network swapped in by _model_change may carry its own copies of the
+    coefficients, which the equation does not use)."""
     lin = [m for m in net.children() if isinstance(m, torch.nn.Linear)]
     params = [q for m in lin for q in (m.weight, m.bias)] + list(coeff_params)
     known = set(map(id, params))
     for name, q in net.named_parameters():
-        if id(q) not in known:
+        if strict and id(q) not in known:
             raise NotImplementedError(f'parameter {name!r} is neither a Linear weight or bias nor '
                                       f'a coefficient of the equation')
     return params
@@ -90,7 +92,9 @@ class DevicePlan:
         self.widths = list(widths)
         streams, sites, parts, factors, terms, groups, slots = [], [], [], [], [], [], []
         self.arrays = []
+        self.array_maps = []         # per problem: IR array key -> plan array index
         self.group_out = []          # per problem: list of (group, output offset) in IR order
+        first_upload = {}            # id(ir) -> its array map; a repeated IR shares its arrays
         out_off = 0
         n_coeff = {len(ir.coeff_params) for ir in irs}
         if len(n_coeff) != 1:
@@ -98,8 +102,17 @@ class DevicePlan:
                              'coefficients')
         self.n_coeff = n_coeff.pop()
         for prob, ir in enumerate(irs):
-            base = len(self.arrays)
-            self.arrays += [a.to(device).reshape(-1).contiguous() for a in ir.arrays]
+            own = {g.row_weight for g in ir.groups if g.row_weight is not None}
+            shared = first_upload.get(id(ir))
+            amap = {}
+            for k, a in enumerate(ir.arrays):
+                if shared is not None and k not in own:
+                    amap[k] = shared[k]
+                else:
+                    amap[k] = len(self.arrays)
+                    self.arrays.append(a.to(device).reshape(-1).contiguous())
+            first_upload.setdefault(id(ir), amap)
+            self.array_maps.append(amap)
             slot_base = len(slots)
             slots += [(prob, w, wn) for (_, w, wn) in ir.slots]
             offs = []
@@ -111,7 +124,7 @@ class DevicePlan:
                         ax = list(axes) + [0] * (_lib.MAX_ORDER - len(axes))
                         streams.append(_lib.StreamDesc(len(axes), (ctypes.c_int32 * 3)(*ax)))
                     off = list(s.offset) + [0.0] * (_lib.MAX_DIN - len(s.offset))
-                    sites.append(_lib.SiteDesc(base + s.points, st_first, len(s.streams),
+                    sites.append(_lib.SiteDesc(amap[s.points], st_first, len(s.streams),
                                                (ctypes.c_float * _lib.MAX_DIN)(*off)))
                 term_first = len(terms)
                 for coeff, output, fl in g.terms:
@@ -127,9 +140,9 @@ class DevicePlan:
                         terms.append(_lib.TermDesc(f_first, len(fl), output, -1, coeff.scale,
                                                    coeff.index))
                     else:
-                        terms.append(_lib.TermDesc(f_first, len(fl), output, base + coeff, 0.0, -1))
-                tgt = -1 if g.target is None else base + g.target
-                rw = -1 if g.row_weight is None else base + g.row_weight
+                        terms.append(_lib.TermDesc(f_first, len(fl), output, amap[coeff], 0.0, -1))
+                tgt = -1 if g.target is None else amap[g.target]
+                rw = -1 if g.row_weight is None else amap[g.row_weight]
                 groups.append(_lib.GroupDesc(prob, g.n_rows, site_first, len(g.sites), term_first,
                                              len(g.terms), g.n_outputs, slot_base + g.slot_first,
                                              tgt, rw, out_off))
@@ -279,6 +292,7 @@ class Solution:
         self.mode = mode
         self.grid = grid
         self.lambda_operator, self.lambda_bound = lambda_operator, lambda_bound
+        self.precision, self.form = precision, form
         widths = mlp_widths(model)
         if batch_size is not None and mode == 'NN' and tol:
             raise NotImplementedError("the causal loss with mini-batches in 'NN' mode (the "
@@ -291,7 +305,9 @@ class Solution:
         self.flat = flatten_parameters(self.params, self.device)
         self._shapes = [(p.shape, p.numel()) for p in self.params]
         self.batches = None if batch_size is None else _Batches(grid.shape[0], batch_size)
-        self._plans = {}
+        self._full_ir = self.ir
+        self._irs = {}                # residual rows -> (ProblemIR, [(batch key, full key)])
+        self._row_src = {}
         if self.batches is not None and mode == 'autograd':
             # one plan per batch size (full batches and the last, shorter one), each lowered on
             # placeholder rows that every evaluation overwrites by a gather from the full arrays
@@ -299,40 +315,52 @@ class Solution:
             n_grid = grid.shape[0]
             sizes = sorted({min(batch_size, n_grid - i) for i in range(0, n_grid, batch_size)},
                            reverse=True)
-            self._row_src = {k: self.ir.arrays[k].to(self.device).reshape(-1)
-                             for k in full}
+            self._row_src = {k: self.ir.arrays[k].to(self.device).reshape(-1) for k in full}
             for n in sizes:
                 ir_b = lower(grid[:n], *args, d_out=widths[-1], tol=tol)
                 if len(ir_b.coeff_params) != len(self.ir.coeff_params):
                     raise RuntimeError('batch lowering changed the trainable coefficients')
                 ir_b.coeff_params = self.ir.coeff_params
-                plan = DevicePlan([ir_b], widths, self.device, precision, form)
-                gathers = [(plan.arrays[kb], self._row_src[kf], self.ir.arrays[kf].numel() //
-                            grid.shape[0]) for kb, kf in zip(_residual_row_arrays(ir_b), full)]
-                self._plans[n] = (ir_b, plan, gathers)
+                self._irs[n] = (ir_b, list(zip(_residual_row_arrays(ir_b), full)))
             self._idx = torch.zeros(batch_size, dtype=torch.int64, device=self.device)
-            self.ir, self.plan, _ = self._plans[sizes[0]]
         else:
-            self.plan = DevicePlan([self.ir], widths, self.device, precision, form)
-            self._plans[self.ir.groups[self.ir.residual_group].n_rows] = (self.ir, self.plan, [])
-        self._grad = torch.zeros(self.plan.n_params, device=self.device, dtype=torch.float32)
+            self._irs[self.ir.groups[self.ir.residual_group].n_rows] = (self.ir, [])
         self._loss_buf = torch.zeros(2, device=self.device, dtype=torch.float64)
-        self._out_bufs = {n: torch.zeros(max(1, p.n_outputs_total), device=self.device)
-                          for n, (_, p, _) in self._plans.items()}
-        self._outputs = self._out_bufs[self.ir.groups[self.ir.residual_group].n_rows]
+        self._build_plans(widths)
         self._clone_grad = True
         self.bval_keys = list(self.ir.bc_types)
         self.bval_length = [sum(r for _, r in self.ir.bc_parts[t]) for t in self.ir.bc_types]
         self._true_bval = None
 
+    def _build_plans(self, widths):
+        """Device plans of this problem for an MLP of `widths` (one per residual batch size)."""
+        self._plans = {}
+        n_grid = self.grid.shape[0]
+        for n, (ir, keys) in self._irs.items():
+            plan = DevicePlan([ir], widths, self.device, self.precision, self.form)
+            gathers = [(plan.arrays[plan.array_maps[0][kb]], self._row_src[kf],
+                        self._full_ir.arrays[kf].numel() // n_grid) for kb, kf in keys]
+            self._plans[n] = (ir, plan, gathers)
+        first = next(iter(self._irs))
+        self.ir, self.plan, _ = self._plans[first]
+        self._grad = torch.zeros(self.plan.n_params, device=self.device, dtype=torch.float32)
+        self._out_bufs = {n: torch.zeros(max(1, p.n_outputs_total), device=self.device)
+                          for n, (_, p, _) in self._plans.items()}
+        self._outputs = self._out_bufs[first]
+
     # -- parameters --------------------------------------------------------------------------
     def _model_change(self, new_model):
-        """Swap in another network of the same shape (tedeous/solution.py:109-127)."""
-        if mlp_widths(new_model) != self.plan.widths:
-            raise ValueError('new model has a different shape')
+        """Swap in another network (tedeous/solution.py:109-127). A network of another shape
+        (same inputs and outputs) gets new device plans of this problem."""
+        widths = mlp_widths(new_model)
+        if widths != self.plan.widths:
+            if widths[0] != self.plan.widths[0] or widths[-1] != self.plan.widths[-1]:
+                raise ValueError('new model has other inputs or outputs')
+            self._build_plans(widths)
         self.model = new_model.to(self.device)
-        self.params = device_parameters(self.model, self.ir.coeff_params)
+        self.params = device_parameters(self.model, self.ir.coeff_params, strict=False)
         self.flat = flatten_parameters(self.params, self.device)
+        self._shapes = [(p.shape, p.numel()) for p in self.params]
 
     def _sync_params(self):
         if not params_are_views(self.params, self.flat):
@@ -365,7 +393,7 @@ class Solution:
             n_t = int(torch.unique(op0).numel())
             if res.n_rows % n_t:
                 n_t = res.n_rows
-        w = self.plan.arrays[res.row_weight]
+        w = self.plan.arrays[self.plan.array_maps[0][res.row_weight]]
         _lib.check(_lib.load().tdg_causal_weights(
             self._outputs.data_ptr() + 4 * off, res.n_rows, ir.n_eq, n_t, tol, w.data_ptr(),
             torch.cuda.current_stream(self.device).cuda_stream), 'tdg_causal_weights')
@@ -393,6 +421,60 @@ class Solution:
             self.loss = self._loss_buf[0:1].to(torch.float32)
             self.loss_normalized = self._loss_buf[1:2].to(torch.float32)
         return self.loss, self.loss_normalized
+
+    def evaluate_many(self, models):
+        """(loss, loss_normalized) of each network on this problem as an (n, 2) float64 device
+        tensor. The reference's cache lookup evaluates cached networks one at a time
+        (tedeous/callbacks/cache.py:133-171: _model_change, then evaluate(save_graph=False)); here
+        the networks of one shape form the parameter sets of one plan over this problem, so one
+        forward-only launch evaluates all of them (the causal loss adds its weight pass). The
+        trainable coefficients keep this solution's current values for every network, as in
+        the reference, whose equation keeps its own parameters across _model_change. In
+        mini-batch mode the networks are evaluated one after another, each on the next batch,
+        as the reference does."""
+        models = list(models)
+        out = torch.zeros(len(models), 2, dtype=torch.float64, device=self.device)
+        if self.batches is not None:
+            keep = self.model
+            for i, m in enumerate(models):
+                self._model_change(m)
+                loss, lossn = self.evaluate(save_graph=False)
+                out[i, 0], out[i, 1] = loss[0], lossn[0]
+            self._model_change(keep)
+            return out
+        self._sync_params()
+        n_coeff = len(self.ir.coeff_params)
+        theta = self.flat[self.flat.numel() - n_coeff:] if n_coeff else None
+        by_shape = {}
+        for i, m in enumerate(models):
+            by_shape.setdefault(tuple(mlp_widths(m)), []).append(i)
+        lib = _lib.load()
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        for widths, idx in by_shape.items():
+            plan = DevicePlan([self.ir] * len(idx), widths, self.device, self.precision, self.form)
+            P = plan.n_params
+            flat = torch.empty(len(idx), P, dtype=torch.float32, device=self.device)
+            for j, i in enumerate(idx):
+                lin = device_parameters(models[i], strict=False)
+                flat[j, :P - n_coeff] = torch.cat([q.detach().reshape(-1).to(self.device, torch.float32)
+                                                   for q in lin])
+                if n_coeff:
+                    flat[j, P - n_coeff:] = theta
+            loss = torch.zeros(2 * len(idx), dtype=torch.float64, device=self.device)
+            outputs = torch.zeros(max(1, plan.n_outputs_total), device=self.device)
+            if self.ir.causal is not None:
+                tol, n_t = self.ir.causal
+                res = self.ir.groups[self.ir.residual_group]
+                plan.loss(flat, loss, outputs)
+                for j in range(len(idx)):
+                    off = plan.group_out[j][self.ir.residual_group]
+                    w = plan.arrays[plan.array_maps[j][res.row_weight]]
+                    _lib.check(lib.tdg_causal_weights(outputs.data_ptr() + 4 * off, res.n_rows,
+                                                      self.ir.n_eq, n_t, tol, w.data_ptr(), stream),
+                               'tdg_causal_weights')
+            plan.loss(flat, loss, outputs)
+            out[torch.tensor(idx, device=self.device)] = loss.view(-1, 2)
+        return out
 
     # -- fields read by callbacks ------------------------------------------------------------
     @property
