@@ -1085,17 +1085,40 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const float* Wl = pbuf + PB_WL;
       float* dW = grad + A.w_off[L - 1];
       float* db = grad + A.b_off[L - 1];
-      // one task per (output, input neuron) and one per output bias (k == K)
-      for (int e = tid; e < d_out * (K + 1); e += NTC) {
-        const int o = e / (K + 1), k = e - o * (K + 1);
-        float sum = 0.f;
-        if (k < K) {
-          for (int r = 0; r < R; ++r) sum = fmaf(gybuf[r * MAX_OUT + o], P1[r * LDS + k], sum);
-          red_add1(&dW[(int64_t)o * K + k], sum);
-        } else {
-          for (int r = 0; r < R; ++r)
-            if (row_v[r]) sum += gybuf[r * MAX_OUT + o];
-          red_add1(&db[o], sum);
+      // dW = dL/dY^T . H_{L-1} and db = sums of dL/dY over the value rows, a warp per (output,
+      // 32 input neurons) or per output bias. For dW a lane is (row phase c = lane / 8, 4 neurons):
+      // it sums rows c, c + 4, ...; the four phases combine by shuffles in a fixed order, so every
+      // sum has the same order in every tile (K is a multiple of 4: 16-byte vectors and atomics)
+      {
+        const int nkb = (K + 31) / 32;
+        for (int t = warp; t < d_out * (nkb + 1); t += NTC / 32) {
+          const int o = t / (nkb + 1), b = t - o * (nkb + 1);
+          if (b < nkb) {
+            const int c = lane >> 3, k = 32 * b + 4 * (lane & 7);
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < K)
+              for (int r = c; r < R; r += 4) {
+                const float gy = gybuf[r * MAX_OUT + o];
+                const float4 h = ld4(&P1[r * LDS + k]);
+                s = make_float4(fmaf(gy, h.x, s.x), fmaf(gy, h.y, s.y), fmaf(gy, h.z, s.z),
+                                fmaf(gy, h.w, s.w));
+              }
+#pragma unroll
+            for (int m = 8; m <= 16; m <<= 1) {
+              s.x += __shfl_xor_sync(0xffffffffu, s.x, m);
+              s.y += __shfl_xor_sync(0xffffffffu, s.y, m);
+              s.z += __shfl_xor_sync(0xffffffffu, s.z, m);
+              s.w += __shfl_xor_sync(0xffffffffu, s.w, m);
+            }
+            if (c == 0 && k < K) red_add4(&dW[(int64_t)o * K + k], s.x, s.y, s.z, s.w);
+          } else {
+            float s = 0.f;
+            for (int r = lane; r < R; r += 32)
+              if (row_v[r]) s += gybuf[r * MAX_OUT + o];
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+            if (lane == 0) red_add1(&db[o], s);
+          }
         }
       }
       __syncthreads();
