@@ -1358,12 +1358,22 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       // tile, so the accumulation order is fixed.
       {
         float4* stage = reinterpret_cast<float4*>(opA);
-        for (int c = 8 * cgrp; c < kp; c += 8 * NCG) {
-          float v[8];
-          tmem_ld8(D2 + lane_addr + c, v);
-          const int j = c >> 2, sw = lrow & 7;
+        const int sw = lrow & 7;
+        auto put = [&](int c, const float (&v)[8]) {
+          const int j = c >> 2;
           stage[lrow * 32 + (j ^ sw)] = make_float4(v[0], v[1], v[2], v[3]);
           stage[lrow * 32 + ((j + 1) ^ sw)] = make_float4(v[4], v[5], v[6], v[7]);
+        };
+        for (int c = 8 * cgrp; c < kp; c += 16 * NCG) {   // two column chunks per wait
+          float v[8], w[8];
+          if (c + 8 * NCG < kp) {
+            tmem_ld8x2(D2 + lane_addr + c, D2 + lane_addr + c + 8 * NCG, v, w);
+            put(c, v);
+            put(c + 8 * NCG, w);
+          } else {
+            tmem_ld8(D2 + lane_addr + c, v);
+            put(c, v);
+          }
         }
         __syncthreads();
         float* dW = grad + A.w_off[l - 1];
