@@ -308,6 +308,12 @@ def allen_cahn_ag(api, n=20, seed=7, dtype='float32', tol=10.0, batch_size=None,
     return domain, bnd, eq, net, kw
 
 
+def _with_kw(case, **extra):
+    """A case with more compile / Model arguments (tol, batch_size)."""
+    domain, bnd, eq, net, kw = case
+    return domain, bnd, eq, net, dict(kw, **extra)
+
+
 def heat_causal_nn(api, n=12, dtype='float32', tol=1.0):
     """The 'NN' heat problem with the causal loss (the first variable, x, plays time)."""
     domain, bnd, eq, net, kw = heat_nn(api, n=n, dtype=dtype)
@@ -325,6 +331,11 @@ COVERAGE_CASES = {
     'allen_cahn_batch_causal_ag': lambda api, dtype='float32': allen_cahn_ag(api, dtype=dtype,
                                                                              batch_size=64),
     'heat_causal_nn': lambda api, dtype='float32': heat_causal_nn(api, dtype=dtype),
+    # a 3-equation system under the causal loss, and trainable coefficients with mini-batches
+    'kovasznay_causal_ag': lambda api, dtype='float32': _with_kw(
+        kovasznay_ag(api, n=15, dtype=dtype, widths=(2, 32, 32, 32, 3)), tol=0.1),
+    'inverse_burgers_batch_ag': lambda api, dtype='float32': _with_kw(
+        inverse_burgers_ag(api, dtype=dtype), batch_size=100),
 }
 GOLDEN_CASES.update(COVERAGE_CASES)
 

@@ -12,7 +12,8 @@ from helpers import build_model, golden, rel
 @pytest.mark.gpu
 @pytest.mark.parametrize('name', ['heat_nn', 'burgers_ag', 'kdv_ag', 'kovasznay_ag',
                                   'allen_cahn_causal_ag', 'allen_cahn_batch_ag',
-                                  'allen_cahn_batch_causal_ag', 'heat_causal_nn'])
+                                  'allen_cahn_batch_causal_ag', 'heat_causal_nn',
+                                  'kovasznay_causal_ag', 'inverse_burgers_batch_ag'])
 def test_train_curve_and_weights_match_reference(name):
     import torch_de_solver_gb300 as T
     g = golden(name)

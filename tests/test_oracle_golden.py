@@ -31,7 +31,8 @@ def test_oracle_matches_reference(name, dtype):
 
 @pytest.mark.parametrize('name', ['heat_nn', 'burgers_ag', 'kdv_ag', 'inverse_burgers_ag',
                                   'allen_cahn_causal_ag', 'allen_cahn_batch_ag',
-                                  'allen_cahn_batch_causal_ag', 'heat_causal_nn'])
+                                  'allen_cahn_batch_causal_ag', 'heat_causal_nn',
+                                  'kovasznay_causal_ag', 'inverse_burgers_batch_ag'])
 def test_oracle_training_curve(name):
     """Model.train(6) with Adam(lr=1e-3): five closure losses, then the final weights."""
     g = golden(name)
