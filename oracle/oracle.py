@@ -1,6 +1,6 @@
 """CPU oracle for the TEDEouS training hot path (test infrastructure only).
 
-This module is the checker. Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline
+This module is the oracle. Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline
 leg use it; the product package never imports it. It restates, in plain PyTorch on the CPU, the
 reference algorithm for one loss evaluation and its parameter gradient:
 
