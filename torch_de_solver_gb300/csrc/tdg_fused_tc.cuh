@@ -1246,6 +1246,24 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const int n = tid & 127;
         float sb = 0.f;
         for (int e = tid; e < 128 * 32; e += NTC) {
+          if constexpr (TMA_A && X3) {   // lane = neuron n, columns = rows r..r+7 (the same r for the warp)
+            if (e >= 128 * 16) break;
+            const int r = (e >> 7) * 8;
+            float v[8], h[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              v[i] = (n < N && r + i < R) ? P1[(r + i) * LDS + n] : 0.f;
+              if (row_v[r + i]) sb += v[i];
+              h[i] = to_tf32(v[i]);
+            }
+            tmem_st8(AHI + lane_addr + r, h);
+            if (X3) {
+#pragma unroll
+              for (int i = 0; i < 8; ++i) v[i] -= h[i];
+              tmem_st8(ALO + lane_addr + r, v);
+            }
+            continue;
+          }
           const int r = (e >> 7) * 4;
           float v[4];
 #pragma unroll
@@ -1254,9 +1272,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             if (row_v[r + i]) sb += v[i];
           }
           if constexpr (TMA_A) {   // lane = neuron n, columns = rows r..r+3 (the same r for the warp)
-            const float h0 = to_tf32(v[0]), h1 = to_tf32(v[1]), h2 = to_tf32(v[2]), h3 = to_tf32(v[3]);
-            tmem_st4(AHI + lane_addr + r, h0, h1, h2, h3);
-            if (X3) tmem_st4(ALO + lane_addr + r, v[0] - h0, v[1] - h1, v[2] - h2, v[3] - h3);
+            tmem_st4(AHI + lane_addr + r, to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
           } else {
             put4<BF16>(opA, n, r, 128, make_float4(v[0], v[1], v[2], v[3]));
             if (X3)   // lane = neuron n, columns = rows r..r+3 (the same r for the whole warp)
