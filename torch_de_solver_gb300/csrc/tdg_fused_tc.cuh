@@ -546,11 +546,10 @@ __device__ void rows_to_opT(const float* __restrict__ P, unsigned char* __restri
     float v[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) v[i] = r + i < R ? P[(r + i) * LDS + n] : 0.f;
-    if (X3) {
-      put4<false>(dst, n, rl, nr, make_float4(v[0], v[1], v[2], v[3]));
-      put4<false>(dst + lo_off, n, rl, nr,
-                  make_float4(v[0] - to_tf32(v[0]), v[1] - to_tf32(v[1]), v[2] - to_tf32(v[2]),
-                              v[3] - to_tf32(v[3])));
+    if (X3) {   // hi rounded once, stored as it is; lo = x - hi, rounded by put4
+      const float4 h = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+      *reinterpret_cast<float4*>(dst + ofs(n, rl, nr, 4)) = h;
+      put4<false>(dst + lo_off, n, rl, nr, make_float4(v[0] - h.x, v[1] - h.y, v[2] - h.z, v[3] - h.w));
     } else {
       put4<BF16>(dst, n, rl, nr, make_float4(v[0], v[1], v[2], v[3]));
     }
