@@ -18,7 +18,9 @@ def _solves(k):
 
 
 @pytest.mark.gpu
-def test_batched_solves_match_oracle_and_single_plans():
+@pytest.mark.parametrize('precision', ['fp32', '3xtf32'])
+def test_batched_solves_match_oracle_and_single_plans(precision):
+    """Every solve's own network: the tensor-core kernel packs each problem's hidden weights."""
     import torch_de_solver_gb300 as T
     models, refs = [], []
     for i, sp in _solves(5):
@@ -29,7 +31,7 @@ def test_batched_solves_match_oracle_and_single_plans():
         l, ln, g, _ = O.loss_and_grad(prob, onet)
         refs.append((l, ln, g.numpy()))
     bm = T.BatchedModel(models)
-    bm.compile('autograd', lambda_operator=1, lambda_bound=1)
+    bm.compile('autograd', lambda_operator=1, lambda_bound=1, precision=precision)
     losses = bm.evaluate(with_grad=True).cpu().numpy()
     P = bm.plan.n_params
     grads = bm.grad.view(len(models), P).cpu().numpy()

@@ -114,7 +114,8 @@ def test_unregistered_coefficient_gets_gradient():
 
 
 @pytest.mark.gpu
-def test_batched_inverse_solves_match_oracle():
+@pytest.mark.parametrize('precision', ['fp32', '3xtf32'])
+def test_batched_inverse_solves_match_oracle(precision):
     """Solves with different data and coefficient values in one launch: per-solve loss and
     gradient (device order: network, then coefficients) against the FP64 oracle."""
     import torch_de_solver_gb300 as T
@@ -131,7 +132,7 @@ def test_batched_inverse_solves_match_oracle():
         gr = torch.cat([p.grad.reshape(-1) for p in onet.parameters()]).numpy()
         refs.append((loss, lossn, np.concatenate([gr[2:], gr[:2]])))
     bm = T.BatchedModel(models)
-    bm.compile('autograd', lambda_operator=1, lambda_bound=100)
+    bm.compile('autograd', lambda_operator=1, lambda_bound=100, precision=precision)
     losses = bm.evaluate(with_grad=True).cpu().numpy()
     P = bm.plan.n_params
     grads = bm.grad.view(len(models), P).cpu().numpy()

@@ -701,7 +701,8 @@ __device__ void zero_rows(unsigned char* buf, int r0, int kp, int es) {
 }  // namespace
 
 struct TcArgs {
-  const unsigned char* wpack;                 // packed hidden weights
+  const unsigned char* wpack;                 // packed hidden weights of problem 0
+  int64_t wpack_stride;                       // bytes per problem
   int64_t wfwd_off[TDG_MAX_LAYERS];           // byte offsets of W_j (forward) per Linear j
   int64_t wbwd_off[TDG_MAX_LAYERS];           // byte offsets of W_j^T
   int* err;                                   // set when a bounded wait gives up
@@ -759,24 +760,26 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
   const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
   const int cgrp = warp >> 2;                    // this warp's 8-column chunks c = 8 * (cgrp + NCG * i)
   int cur_group = -1, cur_problem = -1;
+  const unsigned char* wpk = TA.wpack;           // the packed weights of the tile's problem
   // the first bulk copy of hidden GEMM j's forward weights (split TF32: the first [hi | lo] half)
   auto wfwd_first = [&](int j) {
     const uint32_t nk = (uint32_t)p16(A.width[j + 1]) * p16(A.width[j]);
     if constexpr (TMA_A) {   // split TF32: K-half 0 -> opA, K-half 1 -> opB; TF32: all -> opA
-      cx.issue_a(opA, TA.wpack + TA.wfwd_off[j], nk * 4);
-      if (X3) cx.issue(opB, TA.wpack + TA.wfwd_off[j] + nk * 4, nk * 4);
+      cx.issue_a(opA, wpk + TA.wfwd_off[j], nk * 4);
+      if (X3) cx.issue(opB, wpk + TA.wfwd_off[j] + nk * 4, nk * 4);
     } else {
-      cx.issue(opB, TA.wpack + TA.wfwd_off[j], X3 ? nk * 4 : nk * ES);
+      cx.issue(opB, wpk + TA.wfwd_off[j], X3 ? nk * 4 : nk * ES);
     }
   };
   // the first bulk copy of the dX GEMM's B operand (W^T of Linear j): slot A into opA
   auto wbwd_first = [&](int j) {
     const uint32_t nk = (uint32_t)p16(A.width[j + 1]) * p16(A.width[j]);
-    cx.issue_a(opA, TA.wpack + TA.wbwd_off[j], nk * 4);
+    cx.issue_a(opA, wpk + TA.wbwd_off[j], nk * 4);
   };
 
   for (int ti = A.cta_tile_begin[cta]; ti < A.cta_tile_begin[cta + 1]; ++ti) {
     const DevTile tile = A.tiles[ti];
+    wpk = TA.wpack + (int64_t)tile.problem * TA.wpack_stride;
     cx.publish();                    // opB's last generic accesses ordered before the copy below
     if (L > 2) wfwd_first(1);        // overlaps the coordinates, input layer and first jets
     if (tile.group != cur_group) {
@@ -910,11 +913,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const int K = A.width[j], N = A.width[j + 1];
       const int kp = p16(K), np = p16(N);
       if constexpr (TMA_A) {
-        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, TA.wpack + TA.wfwd_off[j], np, kp);
+        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, wpk + TA.wfwd_off[j], np, kp);
       } else if (X3) {
-        gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wfwd_off[j], np, kp);
+        gemm3x(cx, D1, opA, ALO, opB, wpk + TA.wfwd_off[j], np, kp);
       } else {
-        cx.ensure(opB, TA.wpack + TA.wfwd_off[j], (uint32_t)(np * kp * ES));
+        cx.ensure(opB, wpk + TA.wfwd_off[j], (uint32_t)(np * kp * ES));
         gemm_issue<BF16>(D1, opA, opB, np, kp, cx.bar_mma);
         cx.wait_mma();
       }
@@ -1217,7 +1220,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         rows_to_tmem<X3>(P1, AHI, ALO, np, R, lane_addr, lrow, cgrp);   // dL/dZ_l: the dX A operand
         cx.publish();
         if (X3)   // opB (Z_l) is free: K-half 1 of W_{l-1}^T lands while K-half 0's MMAs run
-          cx.issue(opB, TA.wpack + TA.wbwd_off[l - 1] + (uint32_t)kp * np * 4, (uint32_t)kp * np * 4);
+          cx.issue(opB, wpk + TA.wbwd_off[l - 1] + (uint32_t)kp * np * 4, (uint32_t)kp * np * 4);
       } else {
         zero_rows<BF16>(opA, R, np, ES);
         if (X3) {
@@ -1228,11 +1231,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
       // dX: D1[rows x kp] = dL/dZ_l[rows x np] . (W_{l-1}^T packed [kp x np])^T
       if constexpr (TMA_A) {
-        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, TA.wpack + TA.wbwd_off[l - 1], kp, np);
+        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, wpk + TA.wbwd_off[l - 1], kp, np);
       } else if (X3) {
-        gemm3x(cx, D1, opA, ALO, opB, TA.wpack + TA.wbwd_off[l - 1], kp, np);
+        gemm3x(cx, D1, opA, ALO, opB, wpk + TA.wbwd_off[l - 1], kp, np);
       } else {
-        cx.load(opB, TA.wpack + TA.wbwd_off[l - 1], (uint32_t)(kp * np * ES));
+        cx.load(opB, wpk + TA.wbwd_off[l - 1], (uint32_t)(kp * np * ES));
         gemm_issue<BF16>(D1, opA, opB, kp, np, cx.bar_mma);
         cx.wait_mma();
       }
@@ -1425,9 +1428,10 @@ __global__ void pack_weights_kernel(const float* __restrict__ params, TcLaunch t
   const int j = blockIdx.y + 1;   // hidden Linear layers 1..n_layers-2
   const int K = t.width[j], N = t.width[j + 1];
   const int kp = p16(K), np = p16(N);
-  const float* W = params + t.w_off[j];
-  unsigned char* f = t.wpack + t.fwd_off[j];
-  unsigned char* b = t.wpack + t.bwd_off[j];
+  const int prob = blockIdx.z;    // every problem's own weights
+  const float* W = params + (int64_t)prob * t.n_params + t.w_off[j];
+  unsigned char* f = t.wpack + (int64_t)prob * t.wpack_stride + t.fwd_off[j];
+  unsigned char* b = t.wpack + (int64_t)prob * t.wpack_stride + t.bwd_off[j];
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < np * kp; e += gridDim.x * blockDim.x) {
     const int n = e / kp, k = e % kp;
     const float v = (n < N && k < K) ? W[(int64_t)n * K + k] : 0.f;
@@ -1466,11 +1470,12 @@ cudaError_t launch_variant(const FusedArgs& a, const TcLaunch& t, int n_ctas, cu
     attr = true;
   }
   if (a.n_layers > 2) {   // pack this step's hidden weights
-    pack_weights_kernel<BF16, X3><<<dim3(16, a.n_layers - 2), 256, 0, s>>>(a.params, t);
+    pack_weights_kernel<BF16, X3><<<dim3(16, a.n_layers - 2, t.n_problems), 256, 0, s>>>(a.params, t);
     count_launch();
   }
   TcArgs ta{};
   ta.wpack = t.wpack;
+  ta.wpack_stride = t.wpack_stride;
   for (int l = 0; l < TDG_MAX_LAYERS; ++l) { ta.wfwd_off[l] = t.fwd_off[l]; ta.wbwd_off[l] = t.bwd_off[l]; }
   ta.err = t.err;
   fused_tc_kernel<BF16, X3, CM><<<n_ctas, NTC, smem, s>>>(a, ta);

@@ -74,7 +74,7 @@ struct alignas(16) DevGroup {
 
 struct DevTile {
   int32_t group, row0, nvalid, seg;
-  int32_t first_in_seg, pad[3];
+  int32_t first_in_seg, problem, pad[2];   // problem: the group's parameter set
 };
 
 static_assert(sizeof(DevGroup) % 16 == 0, "DevGroup is copied as int4");
@@ -109,13 +109,17 @@ constexpr size_t fused_smem_bytes() {
 
 cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s);
 
-// tensor-core path: packed hidden weights (per hidden Linear j: W_j as an np x kp K-major operand
-// at fwd_off[j] and W_j^T as kp x np at bwd_off[j], widths padded to 16) and a timeout flag
+// tensor-core path: packed hidden weights (per problem p and hidden Linear j: W_j as an np x kp
+// K-major operand at p * wpack_stride + fwd_off[j] and W_j^T as kp x np at p * wpack_stride +
+// bwd_off[j], widths padded to 16) and a timeout flag
 struct TcLaunch {
   bool bf16;
   bool x3;     // split TF32 (hi*hi + hi*lo + lo*hi)
   int cls_main;   // the site class (besides the value-only class 0) the kernel variant carries
   unsigned char* wpack;
+  int64_t wpack_stride;   // bytes of one problem's packed weights
+  int n_problems;
+  int64_t n_params;       // parameters of one problem (the stride of `params`)
   int64_t fwd_off[TDG_MAX_LAYERS], bwd_off[TDG_MAX_LAYERS];
   int64_t w_off[TDG_MAX_LAYERS];
   int32_t width[TDG_MAX_LAYERS + 1];

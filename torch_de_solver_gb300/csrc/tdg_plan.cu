@@ -87,6 +87,7 @@ struct tdg_plan {
   float* d_gy = nullptr;
   double* d_slot_sum = nullptr;
   int64_t wpack_fwd[TDG_MAX_LAYERS] = {0}, wpack_bwd[TDG_MAX_LAYERS] = {0};
+  int64_t wpack_stride = 0;
   int64_t workspace_bytes = 0;
   bool arrays_dirty = false;
 };
@@ -451,7 +452,7 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     p->ginfo.push_back(HostGroupInfo{g.n_rows, S, g.problem});
     const int T = RMAX / S;
     for (int r0 = 0; r0 < g.n_rows; r0 += T)
-      tiles.push_back(DevTile{gi, r0, std::min(T, g.n_rows - r0), 0, 0, {0, 0, 0}});
+      tiles.push_back(DevTile{gi, r0, std::min(T, g.n_rows - r0), 0, 0, g.problem, {0, 0}});
     p->flops_hidden += 3.0 * 2.0 * (double)g.n_rows * S * hidden_pairs;
     p->flops_total += 3.0 * 2.0 * (double)g.n_rows * S * all_pairs;
   }
@@ -555,7 +556,11 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
       p->wpack_bwd[j] = off;
       off += np * kp * es;
     }
-    if ((st = dev_alloc(p, (void**)&p->d_wpack, (size_t)std::max<int64_t>(off, 16)))) { free_plan(p); return st; }
+    p->wpack_stride = off;   // every problem has its own weights
+    if ((st = dev_alloc(p, (void**)&p->d_wpack, (size_t)std::max<int64_t>(off * d.n_problems, 16)))) {
+      free_plan(p);
+      return st;
+    }
   }
   *out = p;
   return TDG_OK;
@@ -652,6 +657,9 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
     t.x3 = p->precision == TDG_PREC_3XTF32;
     t.cls_main = p->cls_main;
     t.wpack = p->d_wpack;
+    t.wpack_stride = p->wpack_stride;
+    t.n_problems = p->n_problems;
+    t.n_params = p->n_params;
     for (int l = 0; l < TDG_MAX_LAYERS; ++l) {
       t.fwd_off[l] = p->wpack_fwd[l];
       t.bwd_off[l] = p->wpack_bwd[l];

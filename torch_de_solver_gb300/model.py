@@ -46,8 +46,11 @@ class Model:
                 lambda_bound: Union[List[float], float], normalized_loss_stop: bool = False,
                 h: float = 0.001, inner_order: str = '1', boundary_order: str = '2',
                 derivative_points: int = 2, weak_form: List[callable] = None, tol: float = 0,
-                removed_domains: list = None, precision: str = 'fp32', form: str = 'fused'):
-        """Arguments as in tedeous/model.py:56-113, plus precision ('fp32') and form ('fused')."""
+                removed_domains: list = None, precision: str = None, form: str = 'fused'):
+        """Arguments as in tedeous/model.py:56-113, plus precision and form ('fused' or 'plain').
+        precision: '3xtf32' (split-TF32 tensor cores at FP32 tolerance; the default of the fused
+        form), 'fp32' (CUDA cores, bitwise reproducible gradient; the plain form's only one),
+        'tf32' or 'bf16'."""
         if weak_form:
             raise NotImplementedError('weak-form losses are not implemented on the device path')
         self.mode = mode
@@ -159,9 +162,10 @@ class BatchedModel:
         self.models = list(models)
 
     def compile(self, mode: str, lambda_operator, lambda_bound, h: float = 0.001,
-                inner_order: str = '1', boundary_order: str = '2', precision: str = 'fp32'):
+                inner_order: str = '1', boundary_order: str = '2', precision: str = None):
         from .prepare import lower
-        from .solution import DevicePlan, device_parameters, flatten_parameters, mlp_widths
+        from .solution import (DevicePlan, default_precision, device_parameters,
+                               flatten_parameters, mlp_widths)
         if not torch.cuda.is_available():
             raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
         dev = torch.device('cuda', torch.cuda.current_device())
@@ -176,7 +180,7 @@ class BatchedModel:
                              lambda_bound, h, inner_order, boundary_order, d_out=widths[-1]))
         self.mode = mode
         self.irs = irs
-        self.plan = DevicePlan(irs, widths, dev, precision)
+        self.plan = DevicePlan(irs, widths, dev, default_precision(precision, 'fused'))
         P = self.plan.n_params
         for m in self.models:
             m.net.to(dev)

@@ -19,6 +19,14 @@ from . import _lib
 from .prepare import CoeffParam, lower
 
 
+def default_precision(precision, form):
+    """None selects split TF32 ('3xtf32', FP32 tolerance on the tensor cores) for the fused form
+    and FP32 for the plain form, which computes in FP32 only."""
+    if precision is not None:
+        return precision
+    return '3xtf32' if form == 'fused' else 'fp32'
+
+
 def mlp_widths(net):
     """Widths of a torch.nn.Sequential of Linear layers separated by Tanh."""
     mods = list(net.children()) if isinstance(net, torch.nn.Sequential) else None
@@ -283,7 +291,7 @@ class Solution:
     a plan made for that batch size; 'NN' terms ignore the batch, as the reference's do."""
 
     def __init__(self, grid, operator, bconds, model, mode, lambda_operator, lambda_bound,
-                 h=0.001, inner_order='1', boundary_order='2', precision='fp32', form='fused',
+                 h=0.001, inner_order='1', boundary_order='2', precision=None, form='fused',
                  device=None, tol=0, batch_size=None):
         if not torch.cuda.is_available():
             raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
@@ -292,7 +300,7 @@ class Solution:
         self.mode = mode
         self.grid = grid
         self.lambda_operator, self.lambda_bound = lambda_operator, lambda_bound
-        self.precision, self.form = precision, form
+        self.precision, self.form = default_precision(precision, form), form
         widths = mlp_widths(model)
         if batch_size is not None and mode == 'NN' and tol:
             raise NotImplementedError("the causal loss with mini-batches in 'NN' mode (the "
