@@ -308,6 +308,28 @@ def allen_cahn_ag(api, n=20, seed=7, dtype='float32', tol=10.0, batch_size=None,
     return domain, bnd, eq, net, kw
 
 
+def heat2d_ag(api, n=8, seed=9, dtype='float32'):
+    """2-D heat u_t = 0.1 (u_xx + u_yy) on (x, y, t) in [0, 1]^3: three inputs, u(x, y, 0) =
+    sin(pi x) sin(pi y), zero on the four sides (the sites are 3-axis, so the table-driven jets
+    run)."""
+    domain = api.Domain()
+    domain.variable('x', [0, 1], n, dtype=dtype)
+    domain.variable('y', [0, 1], n, dtype=dtype)
+    domain.variable('t', [0, 1], n, dtype=dtype)
+    bnd = api.Conditions()
+    bnd.dirichlet({'x': [0, 1], 'y': [0, 1], 't': 0},
+                  value=lambda g: torch.sin(np.pi * g[:, 0]) * torch.sin(np.pi * g[:, 1]))
+    for side in ({'x': 0, 'y': [0, 1], 't': [0, 1]}, {'x': 1, 'y': [0, 1], 't': [0, 1]},
+                 {'x': [0, 1], 'y': 0, 't': [0, 1]}, {'x': [0, 1], 'y': 1, 't': [0, 1]}):
+        bnd.dirichlet(side, value=0)
+    eq = api.Equation()
+    eq.add({'du/dt': {'coeff': 1, 'du/dt': [2], 'pow': 1},
+            '-0.1 u_xx': {'coeff': -0.1, 'u_xx': [0, 0], 'pow': 1},
+            '-0.1 u_yy': {'coeff': -0.1, 'u_yy': [1, 1], 'pow': 1}})
+    net = mlp([3, 32, 32, 1], seed, getattr(torch, dtype))
+    return domain, bnd, eq, net, dict(mode='autograd', lambda_operator=1, lambda_bound=10)
+
+
 def _with_kw(case, **extra):
     """A case with more compile / Model arguments (tol, batch_size)."""
     domain, bnd, eq, net, kw = case
@@ -336,6 +358,7 @@ COVERAGE_CASES = {
         kovasznay_ag(api, n=15, dtype=dtype, widths=(2, 32, 32, 32, 3)), tol=0.1),
     'inverse_burgers_batch_ag': lambda api, dtype='float32': _with_kw(
         inverse_burgers_ag(api, dtype=dtype), batch_size=100),
+    'heat2d_ag': lambda api, dtype='float32': heat2d_ag(api, dtype=dtype),
 }
 GOLDEN_CASES.update(COVERAGE_CASES)
 
