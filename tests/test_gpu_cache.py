@@ -27,15 +27,16 @@ def _one_by_one(sol, nets):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('precision', ['fp32', '3xtf32'])
+@pytest.mark.parametrize('precision,form', [('fp32', 'fused'), ('3xtf32', 'fused'),
+                                            ('fp32', 'plain')])
 @pytest.mark.parametrize('name', ['burgers_ag', 'allen_cahn_causal_ag', 'inverse_burgers_ag',
                                   'heat_nn'])
-def test_evaluate_many_equals_one_by_one(name, precision):
+def test_evaluate_many_equals_one_by_one(name, precision, form):
     """Networks of two shapes, each shape in one launch, against one evaluate per network (the
     reference's loop); trainable coefficients keep the solver's values for every network."""
     import torch_de_solver_gb300 as T
     g = golden(name)
-    model = build_model(T, name, weights=g['weights'], precision=precision)
+    model = build_model(T, name, weights=g['weights'], precision=precision, form=form)
     sol = model.solution_cls
     w = [m.in_features for m in model.net if isinstance(m, torch.nn.Linear)][0]
     d_out = [m.out_features for m in model.net if isinstance(m, torch.nn.Linear)][-1]

@@ -32,6 +32,29 @@ def test_train_curve_and_weights_match_reference(name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize('name', ['burgers_ag', 'inverse_burgers_ag', 'allen_cahn_causal_ag',
+                                  'kovasznay_ag'])
+def test_train_at_the_default_precision_matches_reference(name):
+    """The same 5 steps with the default precision (split TF32 on the tensor cores): the fused
+    Adam launch and the CUDA-graph replay of the tensor-core step, including the weight packing
+    and, for the causal loss, the forward and weight passes inside the graph."""
+    import torch_de_solver_gb300 as T
+    g = golden(name)
+    model = build_model(T, name, weights=g['weights'], precision=None)
+    assert model.solution_cls.precision == '3xtf32'
+    seen = []
+
+    class Record(T.Callback):
+        def on_epoch_end(self, logs=None):
+            seen.append(float(self.model.cur_loss.reshape(-1)[0]))
+
+    model.train(T.Optimizer('Adam', {'lr': 1e-3}), 6, callbacks=[Record()])
+    assert rel(seen, g['curve32']) < 1e-5, (seen, g['curve32'])
+    w = torch.nn.utils.parameters_to_vector(model.net.parameters()).detach().cpu().numpy()
+    assert rel(w, g['final32']) < 1e-5, rel(w, g['final32'])
+
+
+@pytest.mark.gpu
 def test_train_with_lbfgs_closure():
     """Optimizer("LBFGS") (LBFGS64, FP64 dots) through the reference closure: the loss decreases."""
     import torch_de_solver_gb300 as T
