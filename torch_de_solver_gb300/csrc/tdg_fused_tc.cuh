@@ -516,7 +516,7 @@ __device__ __noinline__ void rows_from_op_tab(const unsigned char* __restrict__ 
 template <int CM>
 __device__ void jet_rows_from_op(const unsigned char* __restrict__ zs, float* __restrict__ P,
                                  const DevGroup& G, int kp) {
-  const int T = G.T, n4s = kp >> 2;
+  const int n4s = kp >> 2;
   for (int q = 0; q < G.n_sites; ++q) {
     const int base = G.site_streams[q][0];
     if (with_class<CM>(G.site_cls[q], [&](auto cc) {
@@ -565,10 +565,8 @@ template <bool BF16, int CM>
 __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ out,
                              const DevGroup& G, int np, bool inplace, bool also_out,
                              unsigned char* __restrict__ tsave) {
-  const int T = G.T;
   const int n4s = np >> 2;
   for (int q = 0; q < G.n_sites; ++q) {
-    const int ns = G.site_nstreams[q];
     const int base = G.site_streams[q][0];
     // classed site: one loop per class, the dispatch outside it
     if (with_class<CM>(G.site_cls[q], [&](auto cc) {
@@ -1159,7 +1157,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       {
         const int n4s = np >> 2;
         for (int q = 0; q < G.n_sites; ++q) {
-          const int ns = G.site_nstreams[q];
           const int base = G.site_streams[q][0];
           if (with_class<CM>(G.site_cls[q], [&](auto cc) {
                 return with_tile_points<decltype(cc)::value>(G, [&](auto tq) {
