@@ -98,3 +98,41 @@ def test_dot_f64_exact_on_integers():
                                        torch.cuda.current_stream().cuda_stream), 'dot')
     n = 100000
     assert out.item() == n * (n + 1) * (2 * n + 1) / 6
+
+
+@pytest.mark.gpu
+def test_callback_weight_changes_reach_the_captured_step():
+    """A callback that replaces parameter data mid-run (as EarlyStopping's perturbation does):
+    the next step, a CUDA-graph replay by then, trains from the new values."""
+    import torch_de_solver_gb300 as T
+    g = golden('burgers_ag')
+    model = build_model(T, 'burgers_ag', weights=g['weights'], precision=None)
+    seen = {}
+
+    class Perturb(T.Callback):
+        def on_epoch_end(self, logs=None):
+            if self.model.t == 6:
+                with torch.no_grad():
+                    for p in self.model.net.parameters():
+                        p.data = p.data + 1e-3   # new tensors, no longer views of the buffer
+                seen['expected'] = self.model.solution_cls.evaluate(save_graph=False)[0].item()
+                seen['stale'] = float(self.model.cur_loss.reshape(-1)[0])
+            elif self.model.t == 7:
+                seen['got'] = float(self.model.cur_loss.reshape(-1)[0])
+
+    model.train(T.Optimizer('Adam', {'lr': 1e-3}), 9, callbacks=[Perturb()])
+    assert model._graph is None and model.t == 9
+    assert abs(seen['got'] - seen['expected']) <= 1e-6 * abs(seen['expected']), seen
+    assert abs(seen['expected'] - seen['stale']) > 1e-4 * abs(seen['stale']), seen
+
+
+@pytest.mark.gpu
+def test_early_stopping_stops_training():
+    """EarlyStopping in Model.train: an absolute threshold above every loss fires each epoch, so
+    training stops after `patience` epochs."""
+    import torch_de_solver_gb300 as T
+    g = golden('burgers_ag')
+    model = build_model(T, 'burgers_ag', weights=g['weights'], precision=None)
+    model.train(T.Optimizer('Adam', {'lr': 1e-3}), 100,
+                callbacks=[T.EarlyStopping(abs_loss=1e9, patience=4, verbose=False)])
+    assert model.stop_training and model.t == 5

@@ -284,3 +284,116 @@ class Cache(Callback):
     def on_train_begin(self, logs=None):
         self.cache()
         self.model._save_dir = self.cache_dir
+
+
+def _num(x):
+    """A loss as a Python float (tensors detached first)."""
+    import torch
+    return float(x.detach()) if isinstance(x, torch.Tensor) else float(x)
+
+
+class EarlyStopping(Callback):
+    """Stop criteria of the training loop (tedeous/callbacks/early_stopping.py:9-165). Each epoch
+    at most one criterion fires, checked in this order, and adds one "stop ding":
+
+    * window: every `loss_window` epochs a straight line is fitted to the last `loss_window`
+      losses; a slope below `eps` relative to the current loss fires, and perturbs the weights;
+    * patience: `no_improvement_patience` epochs without a new minimum fire, and perturb the
+      weights (after going back to the best network when `save_best`);
+    * absolute: a loss below `abs_loss` fires.
+
+    Training stops once `patience` dings have fired. The perturbation adds
+    (2 * randn - 1) * randomize_parameter to every Linear layer (create_random_fn); the
+    device path copies the new values back into its parameter buffer before the next step."""
+
+    def __init__(self, eps=1e-5, loss_window=100, no_improvement_patience=1000, patience=5,
+                 abs_loss=None, normalized_loss=False, randomize_parameter=1e-5,
+                 info_string_every=None, verbose=True, save_best=False):
+        import numpy as np
+        super().__init__()
+        self.eps = eps
+        self.loss_window = loss_window
+        self.no_improvement_patience = no_improvement_patience
+        self.patience = patience
+        self.abs_loss = abs_loss
+        self.normalized_loss = normalized_loss
+        self.info_string_every = np.inf if info_string_every is None else info_string_every
+        self.verbose = verbose
+        self.save_best = save_best
+        self.best_model = None
+        self._stop_dings = 0
+        self._t_imp_start = 0
+        self._r = create_random_fn(randomize_parameter)
+        self._line = None
+        self.last_loss = None
+
+    def _fit_line(self):
+        import numpy as np
+        self._line = np.polyfit(range(self.loss_window), self.last_loss, 1)
+
+    def _perturb(self):
+        if self.mode in ('NN', 'autograd'):
+            self.model.net.apply(self._r)
+
+    def _fired(self):
+        """The criterion that fires this epoch, or None."""
+        loss = _num(self.model.cur_loss)
+        if self.t % self.loss_window == 0:
+            self._fit_line()
+            if abs(self._line[0] / loss) < self.eps and self.t > 0:
+                self._perturb()
+                return 'window_check'
+        if self.t - self._t_imp_start == self.no_improvement_patience:
+            self._t_imp_start = self.t
+            if self.mode in ('NN', 'autograd') and self.save_best:
+                self.model.net = self.best_model
+            self._perturb()
+            return 'patience_check'
+        if self.abs_loss is not None and loss < self.abs_loss:
+            return 'absloss_check'
+        return None
+
+    def _state_line(self):
+        import datetime
+        if self._line is None:
+            self._fit_line()
+        loss = _num(self.model.cur_loss)
+        return ('[{}] Step = {} loss = {:.6f} normalized loss line= {:.6f}x+{:.6f}. There was {} '
+                'stop dings already.'.format(datetime.datetime.now(), self.t, loss,
+                                             self._line[0] / loss, self._line[1] / loss,
+                                             self._stop_dings))
+
+    def on_epoch_begin(self, logs=None):
+        import numpy as np
+        self.t = self.model.t
+        self.mode = self.model.mode
+        self._check = self.model._check
+        if self.last_loss is None:   # the first epoch fills the window with the initial loss
+            self.last_loss = np.zeros(self.loss_window) + _num(self.model.min_loss)
+        else:
+            self.last_loss[(self.t - 3) % self.loss_window] = _num(self.model.cur_loss)
+
+    def on_epoch_end(self, logs=None):
+        import datetime
+        if self._check is None:
+            self._check = self._fired()
+            if self._check is not None:
+                self._stop_dings += 1
+        if self.model.cur_loss < self.model.min_loss:
+            self.model.min_loss = self.model.cur_loss
+            if self.save_best:
+                self.best_model = self.model.net
+            self._t_imp_start = self.t
+        if self.t % self.info_string_every == 0:
+            print(self._state_line())
+        if self.verbose and self._check is not None:
+            print({'window_check': '[{}] Oscillation near the same loss',
+                   'patience_check': '[{}] No improvement in {} steps',
+                   'absloss_check': '[{}] Absolute value of loss is lower than threshold'}[
+                       self._check].format(datetime.datetime.now(), self.no_improvement_patience))
+            print(self._state_line())
+        if self._stop_dings >= self.patience:
+            self.model.stop_training = True
+            if self.save_best:
+                self.model.net = self.best_model
+        self._check = None

@@ -41,6 +41,7 @@ class Model:
         self.batch_size = batch_size
         self._save_dir = os.path.join(tempfile.gettempdir(), 'tedeous_cache/')
         self._graph = None
+        self._check = None   # read by EarlyStopping (tedeous/model.py:46)
 
     def compile(self, mode: str, lambda_operator: Union[List[float], float],
                 lambda_bound: Union[List[float], float], normalized_loss_stop: bool = False,
@@ -84,10 +85,10 @@ class Model:
     def _fused_step(self, capture: bool):
         """loss+gradient, Adam; returns the (1,) loss seen before the update."""
         sol, opt = self.solution_cls, self.optimizer
+        sol._sync_params()   # a callback may have replaced parameter data; the buffer stays put
         if self._graph is not None:
             self._graph.replay()
             return self._loss32[0:1]
-        sol._sync_params()
         sol._launch(with_grad=True)
         opt.apply(sol._grad)
         if capture:

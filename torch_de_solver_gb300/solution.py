@@ -371,8 +371,24 @@ class Solution:
         self._shapes = [(p.shape, p.numel()) for p in self.params]
 
     def _sync_params(self):
-        if not params_are_views(self.params, self.flat):
+        """Parameters whose data a caller replaced (`p.data = ...`, as the reference's
+        randomisation in callbacks does) are copied back into the flat buffer and seated as its
+        views again. The buffer keeps its address, so a captured training step, the fused Adam
+        state and the plans stay valid."""
+        if params_are_views(self.params, self.flat):
+            return
+        if sum(p.numel() for p in self.params) != self.flat.numel():
             self.flat = flatten_parameters(self.params, self.device)
+            return
+        off = 0
+        with torch.no_grad():
+            for p in self.params:
+                n = p.numel()
+                view = self.flat[off:off + n].view(p.shape)
+                if p.data.data_ptr() != view.data_ptr():
+                    view.copy_(p.data.reshape(p.shape).to(view))
+                    p.data = view
+                off += n
 
     # -- evaluation --------------------------------------------------------------------------
     def _select_batch(self):
