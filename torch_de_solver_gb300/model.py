@@ -145,6 +145,7 @@ class Model:
             if info_string_every is not None and self.t % info_string_every == 0:
                 print('This parameter info_string_every in train is obstolete, please use callbacks')
         self._graph = None
+        self.solution_cls.check_status()   # a bounded device wait that gave up raises here
         cbs.on_train_end()
         self._model_save(save_model, model_name)
 
@@ -234,4 +235,5 @@ class BatchedModel:
                 with torch.cuda.graph(graph, stream=cap):
                     one_step()
         self._graph = graph
+        _lib.check(lib.tdg_plan_sync_status(self.plan.handle), 'device status')
         return self.loss.view(-1, 2).clone()

@@ -446,6 +446,12 @@ class Solution:
             self.loss_normalized = self._loss_buf[1:2].to(torch.float32)
         return self.loss, self.loss_normalized
 
+    def check_status(self):
+        """Raises TdgError if a kernel of this solution gave up a bounded device wait since the
+        plan was made (its results are then not to be trusted). Synchronises the device."""
+        for _, plan, _ in self._plans.values():
+            _lib.check(_lib.load().tdg_plan_sync_status(plan.handle), 'device status')
+
     def evaluate_many(self, models):
         """(loss, loss_normalized) of each network on this problem as an (n, 2) float64 device
         tensor. The reference's cache lookup evaluates cached networks one at a time
