@@ -35,14 +35,18 @@ L2_BYTES = 129 * 1024 * 1024
 
 WORKLOADS = {
     # name: (case builder name, kwargs at full size, kwargs of the CPU sample, description)
-    'kovasznay': ('kovasznay_ag', dict(n=1023), dict(n=63),
+    'kovasznay': ('kovasznay_ag', dict(n=1023), dict(n=255),
                   'kovasznay_re20_autograd_2-128x5-3_1024x1024'),
     'burgers': ('burgers_ag', dict(n=100), dict(n=100), 'burgers_autograd_2-32x4-1_101x101'),
-    'kdv': ('kdv_ag', dict(nx=255, nt=127), dict(nx=63, nt=31), 'kdv_autograd_2-64x4-1_256x128'),
+    'kdv': ('kdv_ag', dict(nx=255, nt=127), dict(nx=127, nt=63), 'kdv_autograd_2-64x4-1_256x128'),
     'heat': ('heat_nn', dict(n=20), dict(n=20), 'heat_nn_2-100x3-1_21x21'),
     'sweep': ('sweep_ag', dict(n_solves=256), dict(n_solves=2),
               'sweep_256_solves_autograd_2-64x3-1_Nx,Nt~U{16..128}'),
 }
+# the reference's operation sequence (nested autograd.grad, double backward, torch Adam) through
+# ATen/cuBLAS on the GPU: the largest sample that fits beside the rest of the run
+ATEN_SAMPLE = {'kovasznay': dict(n=511), 'burgers': dict(n=100), 'kdv': dict(nx=255, nt=127),
+               'heat': dict(n=20)}
 
 
 def parse():
@@ -55,7 +59,8 @@ def parse():
     ap.add_argument('--points-per-axis', type=int, default=None)
     ap.add_argument('--precision', default='3xtf32', choices=['fp32', '3xtf32', 'tf32', 'bf16'])
     ap.add_argument('--form', default='fused', choices=['fused', 'plain'])
-    ap.add_argument('--cpu-seconds', type=float, default=20.0)
+    ap.add_argument('--no-compare', action='store_true',
+                    help='skip the plain-form and ATen timings of the same workload')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     return ap.parse_args()
 
@@ -88,9 +93,12 @@ def full_kwargs(args):
 
 
 # ----------------------------------------------------------------------------- CPU baseline
-def cpu_baseline(args, max_seconds):
+def cpu_baseline(args, warmup, steps):
     """The oracle (fp32 restatement of the reference path: nested autograd.grad + double backward,
-    torch.optim.Adam) on the host cores, on a bounded sample of the workload."""
+    torch.optim.Adam) on all host cores, on a bounded sample of the workload: `warmup` untimed
+    steps, then `steps` timed ones. The sample's per-point rate stands for the full workload
+    ('extrapolated' when the sample is smaller: the CPU's per-point rate falls as N grows, so
+    the figure flatters the CPU)."""
     import torch
     from oracle import oracle as O
     threads = os.cpu_count() or 1
@@ -109,20 +117,76 @@ def cpu_baseline(args, max_seconds):
             r = prob.evaluate(net)
             r['loss'].backward()
             opt.step()
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    sec = (time.perf_counter() - t0) / max(1, steps)
+    full = full_points(args)
+    scaled = 'extrapolated' if n_pts < full else 'same size'
+    return dict(value=n_pts / sec, unit=UNIT, cores=threads, kind='port',
+                sample=f'{WORKLOADS[args.workload][0]} {kw}: {n_pts} residual points '
+                       f'({scaled}; the workload has {full}), {warmup} + {steps} Adam steps, '
+                       f'{sec * 1e3:.1f} ms/step, torch {torch.__version__} fp32 on {threads} '
+                       f'threads',
+                steps_per_s=1.0 / sec, points=n_pts, scaling=scaled)
+
+
+def full_points(args):
+    """Residual points of the full workload (autograd mode: every grid node)."""
+    import cases
+    if args.workload == 'sweep':
+        return sum(p['nx'] * p['nt'] for p in cases.sweep_params(WORKLOADS['sweep'][1]['n_solves']))
+    kw = full_kwargs(args)
+    if 'nx' in kw:
+        return (kw['nx'] + 1) * (kw['nt'] + 1)
+    if args.workload == 'heat':
+        return (kw['n'] - 1) ** 2   # 'NN' mode: the central points
+    return (kw['n'] + 1) ** 2
+
+
+def aten_reference(args):
+    """The reference's operation sequence on the GPU through ATen/cuBLAS: the oracle (nested
+    autograd.grad per derivative term, double backward, torch.optim.Adam) in FP32 on the CUDA
+    device, at the largest sample of the workload that fits beside the rest of the run. This is
+    the GPU form of the reference's own path (its solver_device('cuda') runs the same ops).
+    Returns a per-point rate with the sample size stated."""
+    import torch
+    from oracle import oracle as O
+    if args.workload not in ATEN_SAMPLE:
+        return None
+    kw = ATEN_SAMPLE[args.workload]
+    prob, net = O.build_problem(builder_for(args.workload, kw), 'float32')
+    prob.to('cuda')
+    net = net.to('cuda')
+    opt = torch.optim.Adam(net.parameters(), lr=1e-3)
+
+    def step():
+        opt.zero_grad()
+        r = prob.evaluate(net)
+        r['loss'].backward()
+        opt.step()
     for _ in range(2):
         step()
-    times = []
-    t_end = time.perf_counter() + max_seconds
-    while len(times) < 3 or (time.perf_counter() < t_end and len(times) < 200):
-        t0 = time.perf_counter()
+    torch.cuda.synchronize()
+    n_steps = 5
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(n_steps):
         step()
-        times.append(time.perf_counter() - t0)
-    sec = statistics.median(times)
-    return dict(value=n_pts / sec, unit=UNIT, cores=threads, kind='port',
-                sample=f'{WORKLOADS[args.workload][0]} {kw}: {n_pts} residual points, '
-                       f'{len(times)} Adam steps, median {sec * 1e3:.1f} ms/step, torch '
-                       f'{torch.__version__} fp32 on {threads} threads',
-                steps_per_s=1.0 / sec, points=n_pts)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / n_steps
+    n_pts = prob.points.shape[0]
+    peak_gb = torch.cuda.max_memory_allocated() / 1e9
+    del prob, net, opt
+    torch.cuda.empty_cache()
+    return {'value': round(n_pts / (ms / 1e3), 1), 'unit': UNIT, 'points': n_pts,
+            'ms_per_step': round(ms, 3),
+            'sample': f'{WORKLOADS[args.workload][0]} {kw}: {n_pts} points, 2 + {n_steps} Adam '
+                      f'steps, FP32 (TF32 matmul off), peak {peak_gb:.0f} GB allocated',
+            'scaling': 'extrapolated' if n_pts < full_points(args) else 'same size'}
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -285,35 +349,35 @@ def run_sweep(args, world):
             'gpu_launches': int(launches), 'clocks': clk.summary(), 'impl': 'ours'}
 
 
-def run_ours(args, rank, world):
-    import numpy as np
-    import torch
+def build_model(args, form, precision):
+    """The workload as a Model of this package, compiled; its Solution, plan and optimizer."""
     import torch_de_solver_gb300 as T
-    from torch_de_solver_gb300 import _lib
-    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
-    torch.cuda.set_device(dev)
-    kw = full_kwargs(args)
-    domain, bnd, eq, net, ckw = builder_for(args.workload, kw)(T)
+    domain, bnd, eq, net, ckw = builder_for(args.workload, full_kwargs(args))(T)
     ckw = dict(ckw)
     model = T.Model(net, domain, eq, bnd)
-    model.compile(ckw.pop('mode'), precision=args.precision, form=args.form, **ckw)
-    sol = model.solution_cls
-    plan = sol.plan
-    n_pts = sol.ir.n_residual_rows
+    model.compile(ckw.pop('mode'), precision=precision, form=form, **ckw)
     opt = T.Optimizer('Adam', {'lr': 1e-3}).optimizer_choice(model.mode, model.net)
-    flush = torch.empty(2 * L2_BYTES // 4, device=dev)
+    return model, model.solution_cls, opt
+
+
+def time_device_steps(sol, opt, warmup, steps, dev, world, flush):
+    """`warmup` untimed steps, then `steps` timed ones (loss+gradient launch, then Adam), L2
+    flushed before each, CUDA events on the launching stream, clocks sampled meanwhile.
+    Returns (ms per step (max over ranks), mean ms of the loss+gradient part, launches, clocks)."""
+    import torch
+    from torch_de_solver_gb300 import _lib
+    plan = sol.plan
     stream = torch.cuda.current_stream(dev)
 
     def device_step():
         plan.loss_grad(sol.flat, sol._grad, sol._loss_buf, sol._outputs)
 
-    # ---- device-resident throughput
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         device_step()
         opt.apply(sol._grad)
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+           torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     launches0 = _lib.launch_count()
     if world > 1:
         torch.distributed.barrier()
@@ -331,7 +395,21 @@ def run_ours(args, rank, world):
     step_ms = [a.elapsed_time(c) for a, _, c in ev]
     kern_ms = [a.elapsed_time(b) for a, b, _ in ev]
     total_ms = max_over_ranks(sum(step_ms), dev)
-    ms_per_step = total_ms / args.steps
+    return total_ms / steps, statistics.mean(kern_ms), launches, clk.summary()
+
+
+def run_ours(args, rank, world):
+    import torch
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    model, sol, opt = build_model(args, args.form, args.precision)
+    plan = sol.plan
+    n_pts = sol.ir.n_residual_rows
+    flush = torch.empty(2 * L2_BYTES // 4, device=dev)
+
+    # ---- device-resident throughput
+    ms_per_step, kern_mean, launches, clocks = time_device_steps(sol, opt, args.warmup, args.steps,
+                                                                 dev, world, flush)
     value = world * n_pts / (ms_per_step / 1e3)
 
     # ---- end to end through the public API with host buffers
@@ -363,8 +441,7 @@ def run_ours(args, rank, world):
     peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
     bf16 = peaks.get('bf16_tflops', 1900.0)
     flops = plan.info.flops_hidden
-    kern_s = statistics.mean(kern_ms) / 1e3
-    achieved = flops / kern_s / 1e12
+    achieved = flops / (kern_mean / 1e3) / 1e12
     # dense TF32 tensor rate = half the measured dense BF16 rate
     peak = bf16 if args.precision == 'bf16' else bf16 / 2.0
     tag = f'{args.form}_{args.precision}_{args.workload}'
@@ -375,7 +452,7 @@ def run_ours(args, rank, world):
                 'kernel': ('tdg::fused_fp32_kernel' if args.precision == 'fp32' else
                            'tdg::fused_tc_kernel (tcgen05)') + ' + reductions'
                 if args.form == 'fused' else 'plain form: all per-layer launches of the step',
-                'kernel_ms': round(statistics.mean(kern_ms), 4),
+                'kernel_ms': round(kern_mean, 4),
                 'algorithmic_flops_per_launch': flops,
                 'peak_source': ('MEASURED_PEAKS.json bf16_tflops' if peaks else 'fallback 1.9 PFLOP/s bf16')
                 + ('' if args.precision == 'bf16' else ' / 2 (dense TF32 = half of BF16)')}
@@ -390,8 +467,45 @@ def run_ours(args, rank, world):
                        'l2': 'flushed between timed steps (256 MiB write)',
                        'parallelism': f'replicas x{world}'},
             'e2e': e2e, 'roofline': roofline, 'gpu_launches': int(launches),
-            'clocks': clk.summary(), 'impl': 'ours'}
+            'clocks': clocks, 'impl': 'ours'}
+    del model, sol, opt, plan
+    torch.cuda.empty_cache()
+
+    if args.form == 'fused' and not args.no_compare:
+        # the plain form (one launch per layer operation, FP32) on the same workload, steps and
+        # warm-up: the fused-vs-plain ratio of the metric
+        pmodel, psol, popt = build_model(args, 'plain', 'fp32')
+        p_ms, _, p_launches, p_clocks = time_device_steps(psol, popt, args.warmup, args.steps,
+                                                          dev, world, flush)
+        line['plain_ms_per_step'] = round(p_ms, 4)
+        line['plain_value'] = round(world * n_pts / (p_ms / 1e3), 1)
+        line['plain_gpu_launches'] = int(p_launches)
+        line['fused_vs_plain'] = round(p_ms / ms_per_step, 3)
+        del pmodel, psol, popt
+        torch.cuda.empty_cache()
+        if rank == 0:
+            torch.cuda.reset_peak_memory_stats()
+            line['aten_reference'] = aten_reference(args)
     return line
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU path (the oracle port) on all host cores, each step a
+    bounded sample of the workload, honouring --steps and --warmup."""
+    base = cpu_baseline(args, args.warmup, args.steps)
+    return {'metric': METRIC, 'value': round(base['value'], 2), 'unit': UNIT,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': round(1e3 / base['steps_per_s'], 3),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': WORKLOADS[args.workload][3],
+                       'collocation_points': base['points'],
+                       'full_workload_points': full_points(args),
+                       'rate': base['scaling']},
+            'impl': 'reference',
+            'cpu_baseline': {k: base[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')},
+            'e2e': {'value': round(base['value'], 2), 'unit': UNIT,
+                    'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
 
 
 def main():
@@ -399,21 +513,8 @@ def main():
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     if args.impl == 'reference':
-        if rank != 0:
-            return
-        base = cpu_baseline(args, args.cpu_seconds)
-        print(json.dumps({'metric': METRIC, 'value': round(base['value'], 2), 'unit': UNIT,
-                          'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-                          'ms_per_step': round(1e3 / base['steps_per_s'], 3),
-                          'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-                          'dtype': 'f32', 'data': 'synthetic',
-                          'config': {'workload': WORKLOADS[args.workload][3],
-                                     'collocation_points': base['points']},
-                          'impl': 'reference',
-                          'cpu_baseline': {k: base[k] for k in ('value', 'unit', 'cores', 'kind',
-                                                                 'sample')},
-                          'e2e': {'value': round(base['value'], 2), 'unit': UNIT,
-                                  'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}))
+        if rank == 0:
+            print(json.dumps(reference_arm(args)))
         return
     import torch
     if world > 1:
@@ -421,7 +522,7 @@ def main():
     line = run_sweep(args, world) if args.workload == 'sweep' else run_ours(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline:
-            line['cpu_baseline'] = {k: v for k, v in cpu_baseline(args, args.cpu_seconds).items()
+            line['cpu_baseline'] = {k: v for k, v in cpu_baseline(args, 1, 3).items()
                                     if k in ('value', 'unit', 'cores', 'kind', 'sample')}
         print(json.dumps(line))
     if world > 1:

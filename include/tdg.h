@@ -231,7 +231,9 @@ tdg_status tdg_selftest_bounded_wait(int32_t max_polls);
 tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float* exp_avg_sq,
                          float* step, int64_t n, const tdg_adam_desc* hp, tdg_stream_t stream);
 
-/* out[0] = sum_i a[i] * b[i] accumulated in FP64 (device double). */
+/* out[0] = sum_i a[i] * b[i] accumulated in FP64 (device double). The first call on a device
+ * allocates a 2.4 KB partial-sum buffer (under a lock, safe from several host threads) that every
+ * later call on that device shares: calls that overlap on the GPU race on it. */
 tdg_status tdg_dot_f64(const float* a, const float* b, int64_t n, double* out,
                        tdg_stream_t stream);
 

@@ -20,6 +20,12 @@ The operation sequence follows the reference (same term order, same MLP calls, s
 gradients), so an fp32 run of this oracle also serves as the timed CPU baseline of that path.
 Parity of this restatement is pinned by tests/test_oracle_golden.py against fixtures produced
 by executing the reference itself (tests/golden/make_golden.py).
+
+For the largest parity cases (a million collocation points) the checker moves a problem to a CUDA
+device (Problem.to) and evaluates the residual in chunks of points (loss_and_grad_chunked): the
+reference's operator loss is a mean over points (tedeous/losses.py:58), so the loss and its
+gradient are sums of per-chunk parts. The arithmetic is the same restatement; only where it runs
+changes.
 """
 
 from copy import deepcopy
@@ -493,12 +499,33 @@ class Problem:
 
     @staticmethod
     def _lambdas(val, lam):
-        """tedeous/input_preprocessing.py:14-43."""
+        """tedeous/input_preprocessing.py:14-43 (on the device of `val`)."""
         if isinstance(lam, torch.Tensor):
-            return lam
+            return lam.to(val.device)
         if isinstance(lam, (int, float)):
-            return (torch.ones(val.shape[-1]) * lam).reshape(1, -1)
-        return torch.tensor(lam).reshape(1, -1)
+            return (torch.ones(val.shape[-1]) * lam).reshape(1, -1).to(val.device)
+        return torch.tensor(lam).reshape(1, -1).to(val.device)
+
+    def to(self, device):
+        """Move every tensor of the prepared problem (grid, points, boundary subgrids and values,
+        per-point coefficients, shifted grids) to `device`. Trainable coefficients stay the
+        caller's parameters."""
+        def mv(x):
+            if isinstance(x, torch.nn.Parameter):
+                return x
+            if isinstance(x, torch.Tensor):
+                return x.to(device)
+            if isinstance(x, list):
+                return [mv(v) for v in x]
+            if isinstance(x, tuple):
+                return tuple(mv(v) for v in x)
+            if isinstance(x, dict):
+                return {k: mv(v) for k, v in x.items()}
+            return x
+        for name in ('grid', 'points', 'grid_dict', 'prep', 'bconds'):
+            if hasattr(self, name):
+                setattr(self, name, mv(getattr(self, name)))
+        return self
 
     def evaluate(self, net):
         """One reference evaluate(): returns op, bval, true_bval, loss, loss_normalized
@@ -534,7 +561,8 @@ class Problem:
         except RuntimeError:
             self.n_t = op.shape[0]
             res = res.reshape(self.n_t, -1)
-        m = torch.triu(torch.ones((self.n_t, self.n_t), dtype=res.dtype), diagonal=1).T
+        m = torch.triu(torch.ones((self.n_t, self.n_t), dtype=res.dtype, device=res.device),
+                       diagonal=1).T
         with torch.no_grad():
             w = torch.exp(-self.tol * (m @ res))
         loss_oper = torch.mean(w * res)
@@ -563,6 +591,56 @@ def loss_and_grad(problem, net):
     r['loss'].backward()
     grad = torch.cat([p.grad.reshape(-1) for p in net.parameters()])
     return float(r['loss'].detach().reshape(-1)[0]), float(r['loss_normalized'].reshape(-1)[0]), grad, r
+
+
+def loss_and_grad_chunked(problem, net, chunk=131072):
+    """loss_and_grad for 'autograd'-mode problems too large for one autograd graph.
+
+    The operator part of the reference loss is sum_eq lambda_eq * mean_N(op_eq^2)
+    (tedeous/losses.py:58, :84-135), so it is accumulated chunk by chunk of residual points: each
+    chunk's residual (the same nested-gradient term evaluation as evaluate(), eval.py:143-193) is
+    squared, summed, scaled by lambda / N and back-propagated on its own; the gradients add up in
+    p.grad. The boundary part is evaluated once in full (eval.py:433-461, losses.py:79). Returns
+    (loss, loss_normalized, flat gradient, per-equation sum of op^2). Per-point tensor
+    coefficients are sliced with their chunk; the causal loss and mini-batches are not covered."""
+    if problem.mode != 'autograd' or problem.tol != 0 or problem.batch_size is not None:
+        raise NotImplementedError('chunked evaluation covers autograd-mode problems without the '
+                                  'causal loss or mini-batches')
+    for p in net.parameters():
+        p.grad = None
+    pts_all = problem.points
+    n = pts_all.shape[0]
+    n_eq = len(problem.prep)
+    lo = None
+    sumsq = torch.zeros(n_eq, dtype=pts_all.dtype, device=pts_all.device)
+    for i0 in range(0, n, chunk):
+        i1 = min(n, i0 + chunk)
+        prep = []
+        for eq in problem.prep:
+            terms = []
+            for c, factors in eq:
+                if isinstance(c, torch.Tensor) and not isinstance(c, torch.nn.Parameter) \
+                        and c.shape[0] == n:
+                    c = c[i0:i1]
+                terms.append((c, factors))
+            prep.append(terms)
+        pts = pts_all[i0:i1].clone()
+        cols = [problem._apply_ag(net, p, pts).reshape(-1, 1) for p in prep]
+        op = torch.cat(cols, 1)
+        if lo is None:
+            lo = problem._lambdas(op, problem.lambda_operator).to(op.dtype)
+        sq = (op ** 2).sum(0)
+        (sq @ lo.reshape(-1) / n).backward()
+        sumsq += sq.detach()
+    bval, true, _, _ = problem.boundary(net)
+    lb = problem._lambdas(bval, problem.lambda_bound).to(bval.dtype)
+    b_mse = torch.mean((bval - true) ** 2, 0)
+    (b_mse @ lb.reshape(-1)).backward()
+    op_mse = sumsq / n
+    loss = float(op_mse @ lo.reshape(-1) + b_mse.detach() @ lb.reshape(-1))
+    lossn = float(op_mse.sum() + b_mse.detach().sum())
+    grad = torch.cat([p.grad.reshape(-1) for p in net.parameters()])
+    return loss, lossn, grad, sumsq
 
 
 def train_adam(problem, net, lr, epochs):

@@ -1,7 +1,8 @@
 """Generate golden fixtures by running the reference TEDEouS package itself on CPU.
 
-Usage (needs the reference source tree; run from the repository root):
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+Usage (needs the reference source tree, given as the first argument or in TEDEOUS_REFERENCE;
+run from the repository root):
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <path to the reference> [case ...]
 
 For each case in tests/cases.py GOLDEN_CASES this writes tests/golden/<case>.npz holding
   weights      the seeded initial parameters (fp32, flattened in net.parameters() order)
@@ -94,11 +95,11 @@ def run_curve(api, builder, steps=5):
     return np.array(seen), flat(m.net.parameters()).astype(np.float32)
 
 
-def main(ref_path):
+def main(ref_path, only):
     import cases
     api = load_reference(ref_path)
     torch.set_num_threads(min(8, os.cpu_count() or 1))
-    only = sys.argv[2:] or list(cases.GOLDEN_CASES)
+    only = only or list(cases.GOLDEN_CASES)
     for name in only:
         builder = cases.GOLDEN_CASES[name]
         r32 = run_case(api, builder, 'float32')
@@ -121,5 +122,18 @@ def main(ref_path):
               f'n_op={op.shape[0]} keys={r64["bval_keys"]} curve={curve}')
 
 
+def _args():
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument('reference', nargs='?', default=os.environ.get('TEDEOUS_REFERENCE'),
+                    help='root of the reference source tree (or set TEDEOUS_REFERENCE)')
+    ap.add_argument('cases', nargs='*', help='cases to regenerate (default: all)')
+    a = ap.parse_args()
+    if not a.reference:
+        ap.error('the path of the reference source tree is required')
+    return a
+
+
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    a = _args()
+    main(a.reference, a.cases)

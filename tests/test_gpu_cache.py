@@ -1,5 +1,7 @@
 """Cache interop: many cached networks evaluated on one problem in one launch per network shape
-(Solution.evaluate_many) and the Cache callback built on it (tedeous/callbacks/cache.py)."""
+(Solution.evaluate_many), against one evaluate per network and against the FP64 oracle, and the
+Cache callback built on it (tedeous/callbacks/cache.py)."""
+import copy
 import glob
 import os
 
@@ -9,6 +11,7 @@ import torch
 
 import cases
 from helpers import build_model, golden, rel
+from oracle import oracle as O
 
 
 def _nets(widths_list, seed0=100):
@@ -46,6 +49,13 @@ def test_evaluate_many_equals_one_by_one(name, precision, form):
     ref = _one_by_one(sol, nets)
     assert rel(many[:, 0], ref[:, 0]) < 1e-5, (many, ref)
     assert rel(many[:, 1], ref[:, 1]) < 1e-5
+    # every network's loss against the FP64 oracle of the same problem and weights (the
+    # problem's own trainable coefficients keep their initial values, as in the solver)
+    for k, net in enumerate(nets):
+        prob, _ = O.build_problem(cases.GOLDEN_CASES[name], 'float64')
+        loss64, lossn64, _, _ = O.loss_and_grad(prob, copy.deepcopy(net).double())
+        assert rel(many[k, 0], loss64) < 1e-5, (k, many[k, 0], loss64)
+        assert rel(many[k, 1], lossn64) < 1e-5, (k, many[k, 1], lossn64)
     l0, _ = sol.evaluate(save_graph=False)   # the solver's own network is untouched
     assert rel(l0.item(), g['loss64']) < 1e-5
 

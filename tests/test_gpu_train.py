@@ -102,7 +102,7 @@ def test_dot_f64_exact_on_integers():
 
 @pytest.mark.gpu
 def test_callback_weight_changes_reach_the_captured_step():
-    """A callback that replaces parameter data mid-run (as EarlyStopping's perturbation does):
+    """A callback that replaces parameter data mid-run (as the reference's EarlyStopping perturbation does):
     the next step, a CUDA-graph replay by then, trains from the new values."""
     import torch_de_solver_gb300 as T
     g = golden('burgers_ag')
@@ -115,7 +115,11 @@ def test_callback_weight_changes_reach_the_captured_step():
                 with torch.no_grad():
                     for p in self.model.net.parameters():
                         p.data = p.data + 1e-3   # new tensors, no longer views of the buffer
-                seen['expected'] = self.model.solution_cls.evaluate(save_graph=False)[0].item()
+                # the loss of the new values from a separate model, so that nothing here makes
+                # the training model's Solution copy the values back: the step itself must
+                w = torch.cat([p.data.reshape(-1) for p in self.model.net.parameters()]).cpu()
+                other = build_model(T, 'burgers_ag', weights=w.numpy(), precision=None)
+                seen['expected'] = other.solution_cls.evaluate(save_graph=False)[0].item()
                 seen['stale'] = float(self.model.cur_loss.reshape(-1)[0])
             elif self.model.t == 7:
                 seen['got'] = float(self.model.cur_loss.reshape(-1)[0])
@@ -127,12 +131,20 @@ def test_callback_weight_changes_reach_the_captured_step():
 
 
 @pytest.mark.gpu
-def test_early_stopping_stops_training():
-    """EarlyStopping in Model.train: an absolute threshold above every loss fires each epoch, so
-    training stops after `patience` epochs."""
+def test_changed_parameter_layout_raises():
+    """A callback that gives a parameter another number of elements: the plans, the captured step
+    and the fused Adam hold the old layout, so the next step raises instead of training stale
+    parameters."""
     import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300 import _lib
     g = golden('burgers_ag')
     model = build_model(T, 'burgers_ag', weights=g['weights'], precision=None)
-    model.train(T.Optimizer('Adam', {'lr': 1e-3}), 100,
-                callbacks=[T.EarlyStopping(abs_loss=1e9, patience=4, verbose=False)])
-    assert model.stop_training and model.t == 5
+
+    class Grow(T.Callback):
+        def on_epoch_end(self, logs=None):
+            if self.model.t == 5:
+                lin = self.model.net[0]
+                lin.bias.data = torch.zeros(lin.bias.numel() + 1, device=lin.bias.device)
+
+    with pytest.raises(_lib.TdgError, match='parameter layout changed'):
+        model.train(T.Optimizer('Adam', {'lr': 1e-3}), 9, callbacks=[Grow()])

@@ -169,24 +169,14 @@ def test_device_parameter_order_and_optimizer_order():
         device_parameters(net, ir.coeff_params)
 
 
-def test_parameter_registr_and_inverse_task(capsys):
-    """parameter_registr registers one-element float32 parameters and puts them in the dict;
-    InverseTask prints name=value of those parameters on its epochs."""
-    import types
+def test_parameter_registr():
+    """parameter_registr registers one-element float32 parameters and puts them in the dict."""
     import torch_de_solver_gb300 as T
     net = cases.mlp([2, 8, 1], 0)
     params = {'lam1': 2.0, 'lam2': 0.2}
     T.parameter_registr(net, params)
     assert params['lam1'] is net.lam1 and params['lam2'] is net.lam2
     assert net.lam1.dtype == torch.float32 and net.lam1.shape == (1,) and net.lam1.requires_grad
-    cb = T.InverseTask(parameters=params, info_string_every=2)
-    cb.set_model(types.SimpleNamespace(t=3, net=net))
-    cb.on_epoch_end()
-    assert capsys.readouterr().out == ''
-    cb.model.t = 4
-    cb.on_epoch_end()
-    out = capsys.readouterr().out
-    assert out.startswith('lam1=2.0 lam2=0.2') and out.strip().endswith(str(net.lam2.item()))
 
 
 def test_causal_time_slices_and_slots():
@@ -238,48 +228,3 @@ def test_model_save_uses_the_reference_cache_file_names(tmp_path):
     ck = torch.load(files[0], weights_only=False)
     assert set(ck) == {'model', 'model_state_dict'}
     assert torch.equal(ck['model'][0].weight, m.net[0].weight)
-
-
-def _early_stopping_run(cb, losses, min_loss):
-    """Drive an EarlyStopping callback through epochs t = 1, 2, ... with the given losses."""
-    import types
-    net = cases.mlp([2, 8, 1], 0)
-    m = types.SimpleNamespace(t=1, mode='autograd', _check=None, min_loss=torch.tensor(min_loss),
-                              cur_loss=torch.tensor(min_loss), net=net, stop_training=False)
-    cb.set_model(m)
-    w0 = torch.nn.utils.parameters_to_vector(net.parameters()).clone()
-    stopped_at = None
-    for t, loss in enumerate(losses, start=1):
-        m.t = t
-        cb.on_epoch_begin()
-        m.cur_loss = torch.tensor(loss)
-        cb.on_epoch_end()
-        if m.stop_training:   # Model.train leaves its loop here
-            stopped_at = t
-            break
-    w1 = torch.nn.utils.parameters_to_vector(net.parameters())
-    return stopped_at, not torch.equal(w0, w1), cb._stop_dings
-
-
-def test_early_stopping_criteria():
-    """The three criteria of tedeous/callbacks/early_stopping.py on scripted losses."""
-    import torch_de_solver_gb300 as T
-    # absolute threshold: a ding every epoch, stop after `patience` of them, no perturbation
-    stop, moved, dings = _early_stopping_run(
-        T.EarlyStopping(abs_loss=1.0, patience=3, verbose=False), [0.5] * 10, 0.4)
-    assert (stop, moved, dings) == (3, False, 3)
-    # no improvement for 5 epochs: one ding at t = 5 (and every 5 after), weights perturbed
-    stop, moved, dings = _early_stopping_run(
-        T.EarlyStopping(no_improvement_patience=5, loss_window=1000, patience=2, verbose=False,
-                        randomize_parameter=1e-3), [2.0] * 12, 1.0)
-    assert (stop, moved, dings) == (10, True, 2)
-    # a flat loss window (slope 0): a ding at t = 10, weights perturbed
-    stop, moved, dings = _early_stopping_run(
-        T.EarlyStopping(loss_window=10, no_improvement_patience=1000, patience=5, verbose=False,
-                        randomize_parameter=1e-3), [1.0] * 12, 1.0)
-    assert (stop, moved, dings) == (None, True, 1)
-    # a steadily falling loss fires nothing
-    stop, moved, dings = _early_stopping_run(
-        T.EarlyStopping(loss_window=10, no_improvement_patience=1000, verbose=False),
-        [1.0 - 0.05 * t for t in range(12)], 1.0)
-    assert (stop, moved, dings) == (None, False, 0)

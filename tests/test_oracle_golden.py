@@ -54,3 +54,18 @@ def test_fd_stencils_match_reference_tables():
     assert sh == [[2, 0], [0, 0], [0, 0], [-2, 0]] and np.allclose(w, [100, -100, -100, 100])
     sh, w = O.stencil([0], 2, 'fb', '2', h)
     assert sh == [[2, 0], [1, 0], [0, 0]] and np.allclose(w, [30, -40, 10])
+
+
+@pytest.mark.parametrize('name', ['kovasznay_ag', 'burgers_ag', 'sweep_ag', 'kdv_ag'])
+def test_chunked_oracle_matches_reference(name):
+    """The chunked evaluation used as the checker at a million points (the residual summed chunk
+    by chunk, tedeous/losses.py:58) reproduces the reference's FP64 loss and gradient."""
+    g = golden(name)
+    prob, net = O.build_problem(cases.GOLDEN_CASES[name], 'float64')
+    set_flat_weights(net, g['weights'])
+    net.to(torch.float64)
+    loss, lossn, grad, sumsq = O.loss_and_grad_chunked(prob, net, chunk=997)
+    assert rel(loss, g['loss64']) < 1e-12
+    assert rel(lossn, g['lossn64']) < 1e-12
+    assert rel(grad.detach().numpy(), g['grad64']) < 1e-12
+    assert rel(sumsq.numpy(), g['op_sumsq64']) < 1e-12

@@ -1,7 +1,14 @@
 """Callback hooks with the reference's interface (tedeous/callbacks/callback.py:3-75,
-tedeous/callbacks/callback_list.py:5-63). Model.train calls on_train_begin, on_epoch_begin,
-on_epoch_end and on_train_end; a callback reads model.cur_loss, model.t, model.net and
-model.solution_cls and may set model.stop_training."""
+tedeous/callbacks/callback_list.py:5-63) and the Cache callback, whose lookup uses the batched
+evaluation of the device path.
+
+Model.train calls on_train_begin, on_epoch_begin, on_epoch_end and on_train_end; a callback reads
+model.cur_loss, model.min_loss, model.t, model.mode, model.net and model.solution_cls and may set
+model.stop_training. These are the attributes the reference's own callbacks
+(tedeous/callbacks/early_stopping.py, inverse_task.py, plot.py) read, so those run against this
+Model unchanged; they are outside the training hot path and are not rebuilt here. A callback may
+replace parameter data (`p.data = ...`): the device path copies the new values into its parameter
+buffer before the next step."""
 
 
 class Callback:
@@ -67,51 +74,35 @@ class CallbackList(Callback):
             cb.on_train_end(logs or {})
 
 
-class InverseTask(Callback):
-    """Prints the trainable equation coefficients every `info_string_every` epochs
-    (tedeous/callbacks/inverse_task.py:8-38): `name=value` for each network parameter named in
-    `parameters`."""
-
-    def __init__(self, parameters: dict, info_string_every=None):
-        super().__init__()
-        self.parameters = parameters
-        self.info_string_every = info_string_every
-
-    def str_param(self):
-        if self.info_string_every is not None and self.model.t % self.info_string_every == 0:
-            names = set(self.parameters)
-            print(''.join(f'{name}={p.item()} ' for name, p in self.model.net.named_parameters()
-                          if name in names))
-
-    def on_epoch_end(self, logs=None):
-        self.str_param()
-
-
-def create_random_fn(eps):
-    """Adds (2 * randn - 1) * eps to the weight and bias of every Linear layer it is applied to
-    (tedeous/utils.py:14-30)."""
+def _perturbation(eps):
+    """A function that, applied to a network, adds (2 * randn - 1) * eps to the weight and then
+    the bias of each of its Linear layers, in module order: the reference's randomisation of a
+    cached network before training (tedeous/utils.py:14-30, applied at
+    tedeous/callbacks/cache.py:326-331), drawing the same random numbers in the same order."""
     import torch
 
-    def randomize_params(m):
-        if isinstance(m, torch.nn.Linear) and m.bias is not None:
-            m.weight.data = m.weight.data + (2 * torch.randn(m.weight.size()) - 1).to(m.weight) * eps
-            m.bias.data = m.bias.data + (2 * torch.randn(m.bias.size()) - 1).to(m.bias) * eps
-    return randomize_params
+    def apply(net):
+        for m in net.modules():
+            if isinstance(m, torch.nn.Linear) and m.bias is not None:
+                for p in (m.weight, m.bias):
+                    noise = 2 * torch.randn(p.shape) - 1
+                    p.data = p.data + noise.to(p) * eps
+    return apply
 
 
-def remove_all_files(folder):
-    """Deletes every file and folder inside `folder` (tedeous/utils.py:100-114)."""
-    import os
+def _empty_folder(folder):
+    """Delete everything inside `folder`, reporting (not raising) what cannot be deleted; the
+    effect of the reference's clear_cache (tedeous/utils.py:100-114)."""
+    import pathlib
     import shutil
-    for filename in os.listdir(folder):
-        path = os.path.join(folder, filename)
+    for entry in pathlib.Path(folder).iterdir():
         try:
-            if os.path.isfile(path) or os.path.islink(path):
-                os.unlink(path)
-            elif os.path.isdir(path):
-                shutil.rmtree(path)
-        except Exception as e:
-            print('Failed to delete %s. Reason: %s' % (path, e))
+            if entry.is_dir() and not entry.is_symlink():
+                shutil.rmtree(entry)
+            else:
+                entry.unlink()
+        except OSError as err:
+            print(f'cache: could not delete {entry}: {err}')
 
 
 def count_output(model):
@@ -122,128 +113,124 @@ def count_output(model):
     return None
 
 
+def _as_layers(net):
+    """The layer stack of a network: the network itself when it is indexable (nn.Sequential),
+    else its `.model` attribute (a wrapper around one); None when it has neither."""
+    import torch
+    if isinstance(net, torch.nn.Sequential):
+        return net
+    inner = getattr(net, 'model', None)
+    return inner if isinstance(inner, torch.nn.Sequential) else None
+
+
 class CachePreprocessing:
-    """Cache lookup and reuse for a compiled Model (tedeous/callbacks/cache.py:38-258). The lookup
-    evaluates every usable cached network on the current problem in one launch per network shape
-    (Solution.evaluate_many) instead of one evaluate per file, and keeps the reference's choice:
-    the first network with the smallest loss, in the order of the files found."""
+    """Cache lookup and reuse for a compiled Model (the behaviour of
+    tedeous/callbacks/cache.py:38-258). The lookup evaluates every usable cached network on the
+    current problem in one launch per network shape (Solution.evaluate_many) instead of one
+    evaluate per file, and keeps the reference's choice: the first network with the smallest
+    loss, in the order of the files found."""
 
     def __init__(self, model):
         self.solution_cls = model.solution_cls
 
     @staticmethod
-    def _cache_files(files, nmodels=None):
+    def _pick(n_files, nmodels):
+        """Indices of the files to consider: all of them in order, or `nmodels` drawn without
+        replacement from numpy's global generator (as the reference draws them)."""
         import numpy as np
         if nmodels is None:
-            return np.arange(len(files))
-        return np.random.choice(len(files), nmodels, replace=False)
+            return list(range(n_files))
+        return list(np.random.choice(n_files, nmodels, replace=False))
 
-    @staticmethod
-    def _model_reform(init_model, model):
+    def _usable(self, net):
+        """Whether a cached network can stand in for the solver's: the same inputs and outputs
+        and a Linear/Tanh stack the device path evaluates."""
+        from .solution import mlp_widths
+        solver = self.solution_cls.model
+        a, b = _as_layers(net), _as_layers(solver)
+        if a is None or b is None:
+            return False
         try:
-            model[0]
+            return (mlp_widths(a)[0] == mlp_widths(b)[0]
+                    and count_output(net) == count_output(solver))
         except Exception:
-            model = model.model
-        try:
-            init_model[0]
-        except Exception:
-            init_model = init_model.model
-        return init_model, model
+            return False
 
     def cache_lookup(self, cache_dir, nmodels=None, save_graph=False, cache_verbose=False):
         """Best cached checkpoint {'model', 'model_state_dict'} by loss, or None. Files are found
-        with the reference's pattern cache_dir + '\\*.tar' (tedeous/callbacks/cache.py:117), which
-        matches the names Model saves under."""
+        with the reference's pattern cache_dir + '\\*.tar' (tedeous/callbacks/cache.py:117),
+        which matches the names Model saves under."""
         import glob
         import torch
-        from .solution import mlp_widths
         files = glob.glob(cache_dir + '\\*.tar')
         if cache_verbose:
-            print(f"The CACHE will be searched among the models in the folder {cache_dir}.")
-        if len(files) == 0:
-            return None
-        solver = self.solution_cls.model
+            print(f'cache: searching {len(files)} saved networks in {cache_dir}')
         candidates = []
-        for i in self._cache_files(files, nmodels):
-            file = files[i]
+        for i in self._pick(len(files), nmodels) if files else []:
             try:
-                checkpoint = torch.load(file, weights_only=False, map_location='cpu')
-            except Exception:
+                ckpt = torch.load(files[i], weights_only=False, map_location='cpu')
+                net = ckpt['model']
+                net.load_state_dict(ckpt['model_state_dict'])
+            except Exception as err:
                 if cache_verbose:
-                    print('Error loading file {}'.format(file))
+                    print(f'cache: skipping {files[i]}: {err}')
                 continue
-            model = checkpoint['model']
-            model.load_state_dict(checkpoint['model_state_dict'])
-            try:
-                solver_model, cache_model = self._model_reform(solver, model)
-            except Exception:
-                if cache_verbose:
-                    print('Error reforming file {}'.format(file))
-                continue
-            if cache_model[0].in_features != solver_model[0].in_features:
-                continue
-            try:
-                if count_output(model) != count_output(solver):
-                    continue
-                mlp_widths(model)
-            except Exception:   # includes networks the device path cannot evaluate
-                continue
-            candidates.append((i, model))
+            if self._usable(net):
+                candidates.append((i, net))
         if not candidates:
             return None
-        losses = self.solution_cls.evaluate_many([m for _, m in candidates])[:, 0].cpu()
+        losses = self.solution_cls.evaluate_many([net for _, net in candidates])[:, 0].cpu()
         best = int(torch.argmin(losses))   # the first of equal minima, as the reference's '<'
-        i, model = candidates[best]
+        i, net = candidates[best]
         if cache_verbose:
-            print('best_model_num={} , loss={}'.format(i, float(losses[best])))
-        return {'model': model, 'model_state_dict': model.state_dict()}
+            print(f'cache: best network is file {i} with loss {float(losses[best])}')
+        return {'model': net, 'model_state_dict': net.state_dict()}
 
-    def scheme_interp(self, trained_model, cache_verbose=False):
-        """Fits the solver's network to the outputs of a cached network of another architecture
-        on the grid with Adam(lr=1e-3) until the mean squared difference is below 1e-5
-        (tedeous/callbacks/cache.py:183-219)."""
+    def scheme_interp(self, trained_model, cache_verbose=False, tol=1e-5, max_steps=100000):
+        """Fit the solver's network to a cached network of another architecture: Adam(lr=1e-3)
+        on the mean squared difference of the two networks' outputs over the grid, until it is
+        at most `tol` or `max_steps` steps have run (the stopping rule of
+        tedeous/callbacks/cache.py:183-219). Plain torch on the device: this runs once, before
+        training, and is not the hot path."""
         import torch
         sol = self.solution_cls
         grid = sol.grid.to(sol.device)
-        model = sol.model
-        trained_model = trained_model.to(sol.device)
-        optimizer = torch.optim.Adam(model.parameters(), lr=0.001)
-        loss = torch.mean(torch.square(trained_model(grid) - model(grid)))
-
-        def closure():
-            optimizer.zero_grad()
-            loss = torch.mean((trained_model(grid) - model(grid)) ** 2)
-            loss.backward()
-            return loss
-        t = 0
-        while loss > 1e-5 and t < 1e5:
-            optimizer.step(closure)
-            loss = torch.mean(torch.square(trained_model(grid) - model(grid)))
-            t += 1
-            if cache_verbose:
-                print('Interpolate from trained model t={}, loss={}'.format(t, loss))
-        sol._model_change(model)
+        net = sol.model
+        with torch.no_grad():
+            target = trained_model.to(sol.device)(grid)
+        opt = torch.optim.Adam(net.parameters(), lr=0.001)
+        for step in range(max_steps + 1):
+            mse = torch.mean((target - net(grid)) ** 2)
+            if cache_verbose and step:
+                print(f'cache: interpolation step {step}, mse {float(mse)}')
+            if step == max_steps or float(mse) <= tol:
+                break
+            opt.zero_grad()
+            mse.backward()
+            opt.step()
+        sol._model_change(net)
 
     def cache_retrain(self, cache_checkpoint, cache_verbose=False):
-        """Same architecture: continue from the cached network; otherwise fit the solver's network
-        to it (tedeous/callbacks/cache.py:221-258)."""
-        import torch
-        model = self.solution_cls.model
+        """Start from the cached network: as it is when its layer widths equal the solver's,
+        otherwise by fitting the solver's network to it (tedeous/callbacks/cache.py:221-258)."""
+        from .solution import mlp_widths
         if cache_checkpoint is None:
             return None
-        if str(cache_checkpoint['model']) == str(model) and isinstance(model, torch.nn.Sequential) \
-                and isinstance(model[0], torch.nn.Linear):
-            model = cache_checkpoint['model']
-            model.load_state_dict(cache_checkpoint['model_state_dict'])
-            model.train()
-            self.solution_cls._model_change(model)
+        cached = cache_checkpoint['model']
+        cached.load_state_dict(cache_checkpoint['model_state_dict'])
+        solver = self.solution_cls.model
+        try:
+            same = mlp_widths(_as_layers(cached)) == mlp_widths(_as_layers(solver))
+        except Exception:
+            same = False
+        if same:
+            cached.train()
+            self.solution_cls._model_change(cached)
             if cache_verbose:
-                print('Using model from cache')
+                print('cache: training continues from the cached network')
         else:
-            cache_model = cache_checkpoint['model']
-            cache_model.load_state_dict(cache_checkpoint['model_state_dict'])
-            cache_model.eval()
-            self.scheme_interp(cache_model, cache_verbose=cache_verbose)
+            cached.eval()
+            self.scheme_interp(cached, cache_verbose=cache_verbose)
 
 
 class Cache(Callback):
@@ -260,140 +247,21 @@ class Cache(Callback):
         self.cache_model = cache_model
         self.model_randomize_parameter = model_randomize_parameter
         if cache_dir == 'tedeous_cache':
-            folder = os.path.join(tempfile.gettempdir(), 'tedeous_cache/')
-            os.makedirs(folder, exist_ok=True)
-            self.cache_dir = folder
-        else:
-            self.cache_dir = cache_dir
+            cache_dir = os.path.join(tempfile.gettempdir(), 'tedeous_cache/')
+            os.makedirs(cache_dir, exist_ok=True)
+        self.cache_dir = cache_dir
         if clear_cache:
-            remove_all_files(self.cache_dir)
-
-    def _cache_nn(self):
-        cache_preproc = CachePreprocessing(self.model)
-        r = create_random_fn(self.model_randomize_parameter)
-        checkpoint = cache_preproc.cache_lookup(cache_dir=self.cache_dir, nmodels=self.nmodels,
-                                                cache_verbose=self.cache_verbose)
-        cache_preproc.cache_retrain(checkpoint, cache_verbose=self.cache_verbose)
-        self.model.solution_cls.model.apply(r)
+            _empty_folder(self.cache_dir)
 
     def cache(self):
         if self.model.mode == 'mat':
             raise NotImplementedError("'mat' mode is not implemented on the device path")
-        return self._cache_nn()
+        pre = CachePreprocessing(self.model)
+        best = pre.cache_lookup(cache_dir=self.cache_dir, nmodels=self.nmodels,
+                                cache_verbose=self.cache_verbose)
+        pre.cache_retrain(best, cache_verbose=self.cache_verbose)
+        _perturbation(self.model_randomize_parameter)(self.model.solution_cls.model)
 
     def on_train_begin(self, logs=None):
         self.cache()
         self.model._save_dir = self.cache_dir
-
-
-def _num(x):
-    """A loss as a Python float (tensors detached first)."""
-    import torch
-    return float(x.detach()) if isinstance(x, torch.Tensor) else float(x)
-
-
-class EarlyStopping(Callback):
-    """Stop criteria of the training loop (tedeous/callbacks/early_stopping.py:9-165). Each epoch
-    at most one criterion fires, checked in this order, and adds one "stop ding":
-
-    * window: every `loss_window` epochs a straight line is fitted to the last `loss_window`
-      losses; a slope below `eps` relative to the current loss fires, and perturbs the weights;
-    * patience: `no_improvement_patience` epochs without a new minimum fire, and perturb the
-      weights (after going back to the best network when `save_best`);
-    * absolute: a loss below `abs_loss` fires.
-
-    Training stops once `patience` dings have fired. The perturbation adds
-    (2 * randn - 1) * randomize_parameter to every Linear layer (create_random_fn); the
-    device path copies the new values back into its parameter buffer before the next step."""
-
-    def __init__(self, eps=1e-5, loss_window=100, no_improvement_patience=1000, patience=5,
-                 abs_loss=None, normalized_loss=False, randomize_parameter=1e-5,
-                 info_string_every=None, verbose=True, save_best=False):
-        import numpy as np
-        super().__init__()
-        self.eps = eps
-        self.loss_window = loss_window
-        self.no_improvement_patience = no_improvement_patience
-        self.patience = patience
-        self.abs_loss = abs_loss
-        self.normalized_loss = normalized_loss
-        self.info_string_every = np.inf if info_string_every is None else info_string_every
-        self.verbose = verbose
-        self.save_best = save_best
-        self.best_model = None
-        self._stop_dings = 0
-        self._t_imp_start = 0
-        self._r = create_random_fn(randomize_parameter)
-        self._line = None
-        self.last_loss = None
-
-    def _fit_line(self):
-        import numpy as np
-        self._line = np.polyfit(range(self.loss_window), self.last_loss, 1)
-
-    def _perturb(self):
-        if self.mode in ('NN', 'autograd'):
-            self.model.net.apply(self._r)
-
-    def _fired(self):
-        """The criterion that fires this epoch, or None."""
-        loss = _num(self.model.cur_loss)
-        if self.t % self.loss_window == 0:
-            self._fit_line()
-            if abs(self._line[0] / loss) < self.eps and self.t > 0:
-                self._perturb()
-                return 'window_check'
-        if self.t - self._t_imp_start == self.no_improvement_patience:
-            self._t_imp_start = self.t
-            if self.mode in ('NN', 'autograd') and self.save_best:
-                self.model.net = self.best_model
-            self._perturb()
-            return 'patience_check'
-        if self.abs_loss is not None and loss < self.abs_loss:
-            return 'absloss_check'
-        return None
-
-    def _state_line(self):
-        import datetime
-        if self._line is None:
-            self._fit_line()
-        loss = _num(self.model.cur_loss)
-        return ('[{}] Step = {} loss = {:.6f} normalized loss line= {:.6f}x+{:.6f}. There was {} '
-                'stop dings already.'.format(datetime.datetime.now(), self.t, loss,
-                                             self._line[0] / loss, self._line[1] / loss,
-                                             self._stop_dings))
-
-    def on_epoch_begin(self, logs=None):
-        import numpy as np
-        self.t = self.model.t
-        self.mode = self.model.mode
-        self._check = self.model._check
-        if self.last_loss is None:   # the first epoch fills the window with the initial loss
-            self.last_loss = np.zeros(self.loss_window) + _num(self.model.min_loss)
-        else:
-            self.last_loss[(self.t - 3) % self.loss_window] = _num(self.model.cur_loss)
-
-    def on_epoch_end(self, logs=None):
-        import datetime
-        if self._check is None:
-            self._check = self._fired()
-            if self._check is not None:
-                self._stop_dings += 1
-        if self.model.cur_loss < self.model.min_loss:
-            self.model.min_loss = self.model.cur_loss
-            if self.save_best:
-                self.best_model = self.model.net
-            self._t_imp_start = self.t
-        if self.t % self.info_string_every == 0:
-            print(self._state_line())
-        if self.verbose and self._check is not None:
-            print({'window_check': '[{}] Oscillation near the same loss',
-                   'patience_check': '[{}] No improvement in {} steps',
-                   'absloss_check': '[{}] Absolute value of loss is lower than threshold'}[
-                       self._check].format(datetime.datetime.now(), self.no_improvement_patience))
-            print(self._state_line())
-        if self._stop_dings >= self.patience:
-            self.model.stop_training = True
-            if self.save_best:
-                self.model.net = self.best_model
-        self._check = None

@@ -1,4 +1,6 @@
 // Reduction, optimizer and dot-product kernels around the fused loss/gradient kernel.
+#include <mutex>
+
 #include "tdg_internal.h"
 
 namespace tdg {
@@ -183,21 +185,36 @@ cudaError_t launch_adam(float* p, const float* g, float* m, float* v, float* ste
   return cudaGetLastError();
 }
 
-// scratch for the two-pass dot product lives in a small per-device buffer allocated once
+// scratch for the two-pass dot product lives in a small per-device buffer allocated once; the
+// first call on a device allocates it under a lock, so concurrent first calls from several host
+// threads neither leak nor hand a kernel a pointer that is still being written. Every later call
+// on that device shares the buffer: calls that overlap on the GPU race on it.
+namespace {
+std::mutex g_dot_mu;
+double* g_dot_partial[64] = {nullptr};
+}  // namespace
+
 cudaError_t launch_dot_f64(const float* a, const float* b, int64_t n, double* out,
                            cudaStream_t s) {
-  static double* partial[64] = {nullptr};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev >= 64) return cudaErrorInvalidDevice;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   constexpr int kBlocks = 304;
-  if (!partial[dev]) {
-    e = cudaMalloc(&partial[dev], kBlocks * sizeof(double));
-    if (e != cudaSuccess) return e;
+  double* partial = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_dot_mu);
+    if (!g_dot_partial[dev]) {
+      e = cudaMalloc(&g_dot_partial[dev], kBlocks * sizeof(double));
+      if (e != cudaSuccess) {
+        g_dot_partial[dev] = nullptr;
+        return e;
+      }
+    }
+    partial = g_dot_partial[dev];
   }
-  dot_f64_kernel<<<kBlocks, 256, 0, s>>>(a, b, n, partial[dev]);
-  dot_finish_kernel<<<1, 32, 0, s>>>(partial[dev], kBlocks, out);
+  dot_f64_kernel<<<kBlocks, 256, 0, s>>>(a, b, n, partial);
+  dot_finish_kernel<<<1, 32, 0, s>>>(partial, kBlocks, out);
   count_launch(2);
   return cudaGetLastError();
 }

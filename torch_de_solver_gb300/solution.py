@@ -378,8 +378,11 @@ class Solution:
         if params_are_views(self.params, self.flat):
             return
         if sum(p.numel() for p in self.params) != self.flat.numel():
-            self.flat = flatten_parameters(self.params, self.device)
-            return
+            # the device plans, a captured step and the fused Adam state all hold the old
+            # parameter layout: a changed layout cannot be trained from silently
+            raise _lib.TdgError('the parameter layout changed after compile (another number of '
+                                'parameter elements); swap networks with _model_change or '
+                                'compile again')
         off = 0
         with torch.no_grad():
             for p in self.params:
