@@ -237,6 +237,35 @@ tdg_status tdg_adam_step(float* params, const float* grad, float* exp_avg, float
 tdg_status tdg_dot_f64(const float* a, const float* b, int64_t n, double* out,
                        tdg_stream_t stream);
 
+/* Device-resident L-BFGS, replacing the torch.optim.LBFGS that the reference selects
+ * (tedeous/optimizers/optimizer.py:50-51) in its two-loop recursion and curvature updates.
+ * The history is a ring of history_size + 1 (s, y) pairs of n floats on the device with FP64
+ * rho = 1 / y.s, FP64 two-loop coefficients and the FP64 scale H_diag = y.s / y.y; every dot
+ * product accumulates in FP64 with fixed-order (deterministic) sums. No call synchronises the host
+ * except tdg_lbfgs_create. A state is not thread safe: one per optimizer and stream. */
+typedef struct tdg_lbfgs tdg_lbfgs;
+tdg_status tdg_lbfgs_create(int64_t n, int32_t history_size, tdg_lbfgs** out);
+tdg_status tdg_lbfgs_destroy(tdg_lbfgs* h);
+/* Forget every stored pair; H_diag = 1. */
+tdg_status tdg_lbfgs_reset(tdg_lbfgs* h, tdg_stream_t stream);
+/* The pair y = g - g_prev, s = t d, stored (the oldest dropped when the ring is full) when
+ * y.s > 1e-10, as torch.optim.LBFGS does; otherwise the history is unchanged. */
+tdg_status tdg_lbfgs_push(tdg_lbfgs* h, const float* g, const float* g_prev, const float* d,
+                          double t, tdg_stream_t stream);
+/* d = -H g by the two-loop recursion over the stored pairs (newest first, then oldest first).
+ * n_pairs_bound (<= history_size) is an upper bound on the stored pairs, e.g. the number of pushes
+ * so far: the host need not know how many were accepted. 2 (n_pairs_bound + 1) launches. */
+tdg_status tdg_lbfgs_direction(tdg_lbfgs* h, const float* g, float* d, int32_t n_pairs_bound,
+                               tdg_stream_t stream);
+/* out[0..4] (device doubles) = g.d, sum |g_i|, max |g_i|, max |d_i|, *loss: the quantities of
+ * torch.optim.LBFGS's step-size and stopping tests, for one device-to-host read. d and loss may
+ * be NULL (read as 0). */
+tdg_status tdg_lbfgs_stats(tdg_lbfgs* h, const float* g, const float* d, const float* loss,
+                           double* out, tdg_stream_t stream);
+/* out = x + t d (out may alias x): the parameter update of an L-BFGS step or line-search trial. */
+tdg_status tdg_axpy(const float* x, const float* d, double t, float* out, int64_t n,
+                    tdg_stream_t stream);
+
 /* Allocation-free variant of tdg_dot_f64. No counterpart in the reference: it serves callers that
  * own all device memory themselves (a framework allocator that has reserved the GPU, or a
  * foreign-language host binding this ABI under a fixed device-memory budget) and so cannot let

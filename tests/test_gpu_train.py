@@ -67,29 +67,6 @@ def test_train_with_lbfgs_closure():
 
 
 @pytest.mark.gpu
-def test_lbfgs64_follows_torch_lbfgs():
-    """Same closure, same hyper-parameters: LBFGS64 (FP64 dots) and torch.optim.LBFGS (FP32 dots)
-    take the same steps up to dot-product rounding."""
-    import torch_de_solver_gb300 as T
-    g = golden('burgers_ag')
-    finals = []
-    for cls in (T.LBFGS64, torch.optim.LBFGS):
-        model = build_model(T, 'burgers_ag', weights=g['weights'])
-        opt = cls(model.net.parameters(), lr=0.5, max_iter=6, history_size=4)
-        sol = model.solution_cls
-
-        def closure():
-            opt.zero_grad()
-            loss, _ = sol.evaluate()
-            loss.backward()
-            return loss
-        for _ in range(3):
-            opt.step(closure)
-        finals.append(torch.nn.utils.parameters_to_vector(model.net.parameters()).detach().cpu().numpy())
-    assert rel(finals[0], finals[1]) < 1e-4, rel(finals[0], finals[1])
-
-
-@pytest.mark.gpu
 def test_dot_f64_exact_on_integers():
     from torch_de_solver_gb300 import _lib
     a = torch.arange(1, 100001, dtype=torch.float32, device='cuda')

@@ -54,3 +54,18 @@ def test_causal_and_gather_reject_bad_shapes_without_a_gpu():
     assert b'time slices' in lib.tdg_last_error()
     assert lib.tdg_gather_rows(None, 5, None, 0, 2, None, None) == _lib.OK         # nothing to do
     assert lib.tdg_gather_rows(1, 5, 1, 4, 0, 1, None) == _lib.ERR_SHAPE
+
+
+def test_lbfgs_entry_points_validate_on_the_host():
+    """Argument checks of the device L-BFGS run before any allocation or launch."""
+    from torch_de_solver_gb300 import _lib
+    lib = _lib.load()
+    assert lib.tdg_lbfgs_create(10, 4, None) == _lib.ERR_INVALID
+    h = ctypes.c_void_p()
+    assert lib.tdg_lbfgs_create(0, 4, ctypes.byref(h)) == _lib.ERR_SHAPE
+    assert lib.tdg_lbfgs_create(10, 0, ctypes.byref(h)) == _lib.ERR_SHAPE and not h.value
+    assert lib.tdg_lbfgs_push(None, None, None, None, 1.0, None) == _lib.ERR_INVALID
+    assert lib.tdg_lbfgs_direction(None, None, None, 0, None) == _lib.ERR_INVALID
+    assert lib.tdg_lbfgs_stats(None, None, None, None, None, None) == _lib.ERR_INVALID
+    assert lib.tdg_axpy(None, None, 1.0, None, 3, None) == _lib.ERR_INVALID
+    assert lib.tdg_lbfgs_destroy(None) == _lib.OK

@@ -105,6 +105,13 @@ SIGNATURES = {
     'tdg_adam_step': (i32, [vp, vp, vp, vp, vp, i64, ctypes.POINTER(AdamDesc), vp]),
     'tdg_dot_f64': (i32, [vp, vp, i64, vp, vp]),
     'tdg_dot_f64_noalloc': (i32, [vp, vp, i64, vp, vp]),
+    'tdg_lbfgs_create': (i32, [i64, i32, ctypes.POINTER(vp)]),
+    'tdg_lbfgs_destroy': (i32, [vp]),
+    'tdg_lbfgs_reset': (i32, [vp, vp]),
+    'tdg_lbfgs_push': (i32, [vp, vp, vp, vp, ctypes.c_double, vp]),
+    'tdg_lbfgs_direction': (i32, [vp, vp, vp, i32, vp]),
+    'tdg_lbfgs_stats': (i32, [vp, vp, vp, vp, vp, vp]),
+    'tdg_axpy': (i32, [vp, vp, ctypes.c_double, vp, i64, vp]),
     'tdg_causal_weights': (i32, [vp, i64, i32, i64, f32, vp, vp]),
     'tdg_gather_rows': (i32, [vp, i64, vp, i64, i32, vp, vp]),
 }

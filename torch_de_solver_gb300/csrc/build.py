@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
 SOURCES = ['tdg_plan.cu', 'tdg_fused.cu', 'tdg_fused_tc.cu', 'tdg_plain.cu', 'tdg_util.cu',
-           'tdg_noalloc.cu']
+           'tdg_noalloc.cu', 'tdg_lbfgs.cu']
 # the tensor-core kernel: one object per (precision, main site class), from tdg_tc_inst.cu
 TC_PRECISIONS = (('tf32', 0, 0), ('bf16', 1, 0), ('3x', 0, 1))
 TC_CLASSES = 11   # jetcls::N_CLASSES in tdg_jetcls.h
