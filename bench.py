@@ -62,6 +62,9 @@ def parse():
     ap.add_argument('--no-compare', action='store_true',
                     help='skip the plain-form and ATen timings of the same workload')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--optimizer', default='adam', choices=['adam', 'lbfgs'],
+                    help='lbfgs: time L-BFGS iterations (device history, FP64 dots, strong-Wolfe '
+                         'line search) instead of Adam steps')
     return ap.parse_args()
 
 
@@ -489,6 +492,67 @@ def run_ours(args, rank, world):
     return line
 
 
+def run_lbfgs(args, world):
+    """L-BFGS on the workload through the public API (LBFGS64: device-resident history, FP64
+    two-loop dots, strong-Wolfe line search) after `warmup` iterations: the throughput of the
+    loss+gradient launches it drives (closures/s, points/s) and its iterations/s. Host
+    synchronisation happens only for the line search's tests, as in torch.optim.LBFGS."""
+    import torch
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300 import _lib
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    model, sol, _ = build_model(args, args.form, args.precision)
+    n_pts = sol.ir.n_residual_rows
+    counter = [0]
+
+    def make(max_iter):
+        opt = T.LBFGS64(model.net.parameters(), lr=1.0, max_iter=max_iter, history_size=100,
+                        line_search_fn='strong_wolfe', tolerance_grad=0.0, tolerance_change=0.0)
+
+        def closure():
+            counter[0] += 1
+            opt.zero_grad()
+            loss, _ = sol.evaluate()
+            loss.backward()
+            return loss
+        return opt, closure
+    opt, closure = make(args.warmup)
+    opt.step(closure)
+    torch.cuda.synchronize()
+    opt, closure = make(args.steps)
+    counter[0] = 0
+    l0 = _lib.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        t0 = time.perf_counter()
+        opt.step(closure)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+    sec = max_over_ranks(sec, dev)
+    st = opt.state[opt.param_groups[0]['params'][0]]
+    iters, closures = st['n_iter'], counter[0]
+    loss = sol.evaluate(save_graph=False)[0].item()
+    return {'metric': METRIC, 'value': round(world * n_pts * closures / sec, 1), 'unit': UNIT,
+            'n_gpus': world, 'steps': iters, 'warmup': args.warmup,
+            'ms_per_step': round(1e3 * sec / max(1, iters), 4),
+            'steps_per_s': round(iters / sec, 3), 'closures_per_s': round(closures / sec, 3),
+            'ms_per_closure': round(1e3 * sec / max(1, closures), 4),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded grid, closed-form boundary data, seeded torch init)',
+            'config': {'workload': WORKLOADS[args.workload][3], 'collocation_points': n_pts,
+                       'precision': args.precision, 'form': args.form,
+                       'optimizer': 'L-BFGS (LBFGS64: lr 1, history 100, strong Wolfe; '
+                                    'device history, FP64 dots)',
+                       'iterations': iters, 'closures': closures, 'final_loss': loss,
+                       'l2': 'not flushed (inputs and weights stay resident between closures)',
+                       'parallelism': f'replicas x{world}'},
+            'gpu_launches': int(_lib.launch_count() - l0), 'clocks': clk.summary(),
+            'impl': 'ours'}
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU path (the oracle port) on all host cores, each step a
     bounded sample of the workload, honouring --steps and --warmup."""
@@ -519,7 +583,12 @@ def main():
     import torch
     if world > 1:
         torch.distributed.init_process_group('nccl')
-    line = run_sweep(args, world) if args.workload == 'sweep' else run_ours(args, rank, world)
+    if args.workload == 'sweep':
+        line = run_sweep(args, world)
+    elif args.optimizer == 'lbfgs':
+        line = run_lbfgs(args, world)
+    else:
+        line = run_ours(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline:
             line['cpu_baseline'] = {k: v for k, v in cpu_baseline(args, 1, 3).items()

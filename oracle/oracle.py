@@ -593,7 +593,7 @@ def loss_and_grad(problem, net):
     return float(r['loss'].detach().reshape(-1)[0]), float(r['loss_normalized'].reshape(-1)[0]), grad, r
 
 
-def loss_and_grad_chunked(problem, net, chunk=131072):
+def loss_and_grad_chunked(problem, net, chunk=131072, rows=None, with_boundary=True):
     """loss_and_grad for 'autograd'-mode problems too large for one autograd graph.
 
     The operator part of the reference loss is sum_eq lambda_eq * mean_N(op_eq^2)
@@ -602,7 +602,11 @@ def loss_and_grad_chunked(problem, net, chunk=131072):
     squared, summed, scaled by lambda / N and back-propagated on its own; the gradients add up in
     p.grad. The boundary part is evaluated once in full (eval.py:433-461, losses.py:79). Returns
     (loss, loss_normalized, flat gradient, per-equation sum of op^2). Per-point tensor
-    coefficients are sliced with their chunk; the causal loss and mini-batches are not covered."""
+    coefficients are sliced with their chunk; the causal loss and mini-batches are not covered.
+
+    rows=(r0, r1) evaluates only those residual points (still divided by the full point count)
+    and with_boundary=False leaves the boundary part out: the share of one rank when the points
+    are split across devices, whose shares add up to the whole loss and gradient."""
     if problem.mode != 'autograd' or problem.tol != 0 or problem.batch_size is not None:
         raise NotImplementedError('chunked evaluation covers autograd-mode problems without the '
                                   'causal loss or mini-batches')
@@ -613,8 +617,9 @@ def loss_and_grad_chunked(problem, net, chunk=131072):
     n_eq = len(problem.prep)
     lo = None
     sumsq = torch.zeros(n_eq, dtype=pts_all.dtype, device=pts_all.device)
-    for i0 in range(0, n, chunk):
-        i1 = min(n, i0 + chunk)
+    r0, r1 = (0, n) if rows is None else rows
+    for i0 in range(r0, r1, chunk):
+        i1 = min(r1, i0 + chunk)
         prep = []
         for eq in problem.prep:
             terms = []
@@ -627,19 +632,24 @@ def loss_and_grad_chunked(problem, net, chunk=131072):
         pts = pts_all[i0:i1].clone()
         cols = [problem._apply_ag(net, p, pts).reshape(-1, 1) for p in prep]
         op = torch.cat(cols, 1)
-        if lo is None:
-            lo = problem._lambdas(op, problem.lambda_operator).to(op.dtype)
         sq = (op ** 2).sum(0)
+        lo = problem._lambdas(op, problem.lambda_operator).to(op.dtype)
         (sq @ lo.reshape(-1) / n).backward()
         sumsq += sq.detach()
-    bval, true, _, _ = problem.boundary(net)
-    lb = problem._lambdas(bval, problem.lambda_bound).to(bval.dtype)
-    b_mse = torch.mean((bval - true) ** 2, 0)
-    (b_mse @ lb.reshape(-1)).backward()
     op_mse = sumsq / n
-    loss = float(op_mse @ lo.reshape(-1) + b_mse.detach() @ lb.reshape(-1))
-    lossn = float(op_mse.sum() + b_mse.detach().sum())
-    grad = torch.cat([p.grad.reshape(-1) for p in net.parameters()])
+    if lo is None:
+        lo = problem._lambdas(sumsq.reshape(1, -1), problem.lambda_operator).to(sumsq.dtype)
+    loss = float(op_mse @ lo.reshape(-1))
+    lossn = float(op_mse.sum())
+    if with_boundary:
+        bval, true, _, _ = problem.boundary(net)
+        lb = problem._lambdas(bval, problem.lambda_bound).to(bval.dtype)
+        b_mse = torch.mean((bval - true) ** 2, 0)
+        (b_mse @ lb.reshape(-1)).backward()
+        loss += float(b_mse.detach() @ lb.reshape(-1))
+        lossn += float(b_mse.detach().sum())
+    grad = torch.cat([torch.zeros_like(p).reshape(-1) if p.grad is None else p.grad.reshape(-1)
+                      for p in net.parameters()])
     return loss, lossn, grad, sumsq
 
 

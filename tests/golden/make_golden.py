@@ -16,6 +16,10 @@ For each case in tests/cases.py GOLDEN_CASES this writes tests/golden/<case>.npz
   curve32      loss values seen by the closure over 5 Adam(lr=1e-3) steps of Model.train(6)
                (mini-batch cases: the last closure loss of each of the 5 epochs, n_batches steps each)
   final32      parameters after those 5 steps
+With --trained it instead runs the reference's Model.train for the long benchmark runs (C1 heat
+'NN' 2000 epochs, C2 Burgers 'autograd' 5000 epochs, Adam lr=1e-3) and writes
+tests/golden/trained_<case>.npz: the seeded initial weights, the trained solution u on the grid,
+the loss every 100 epochs and the final weights.
 The reference needs one stub: SALib (imported by tedeous/callbacks/adaptive_lambda.py:4) is
 absent, so an empty module is installed in sys.modules before the import.
 """
@@ -95,6 +99,45 @@ def run_curve(api, builder, steps=5):
     return np.array(seen), flat(m.net.parameters()).astype(np.float32)
 
 
+# long training runs of the reference (Model.train with Adam(lr=1e-3), no callbacks besides a
+# loss recorder): the benchmark configs C1 (heat, 'NN', 2000 epochs) and C2 (Burgers, 'autograd',
+# 5000 epochs), seeded; stored as trained_<case>.npz
+TRAINED = {'heat_nn': 2000, 'burgers_ag': 5000}
+
+
+def run_trained(api, builder, epochs, every=100):
+    """Model.train(epochs) of the reference: its solution on the grid afterwards (the network
+    evaluated at every grid node), the loss every `every` epochs and the final weights."""
+    domain, bnd, eq, net, kw = builder(api, dtype='float32')
+    w0 = flat(net.parameters()).astype(np.float32)
+    m = api.Model(net, domain, eq, bnd)
+    mode = kw.pop('mode')
+    m.compile(mode, **kw)
+    seen = []
+
+    class Record(api.Callback):
+        def on_epoch_end(self, logs=None):
+            if self.model.t % every == 0:
+                seen.append((self.model.t, float(self.model.cur_loss.detach().reshape(-1)[0])))
+
+    m.train(api.Optimizer('Adam', {'lr': 1e-3}), epochs, callbacks=[Record()])
+    grid = domain.build(mode)
+    with torch.no_grad():
+        u = m.net(grid).detach().to(torch.float64).numpy()
+    return dict(weights=w0, epochs=epochs, grid=grid.numpy(), u=u,
+                curve=np.array(seen), final=flat(m.net.parameters()).astype(np.float32))
+
+
+def main_trained(ref_path, only):
+    import cases
+    api = load_reference(ref_path)
+    torch.set_num_threads(min(8, os.cpu_count() or 1))
+    for name in only or list(TRAINED):
+        r = run_trained(api, cases.GOLDEN_CASES[name], TRAINED[name])
+        np.savez_compressed(os.path.join(HERE, 'trained_' + name + '.npz'), **r)
+        print(f'trained {name}: {TRAINED[name]} epochs, last losses {r["curve"][-3:].tolist()}')
+
+
 def main(ref_path, only):
     import cases
     api = load_reference(ref_path)
@@ -128,7 +171,9 @@ def _args():
     ap.add_argument('reference', nargs='?', default=os.environ.get('TEDEOUS_REFERENCE'),
                     help='root of the reference source tree (or set TEDEOUS_REFERENCE)')
     ap.add_argument('cases', nargs='*', help='cases to regenerate (default: all)')
-    a = ap.parse_args()
+    ap.add_argument('--trained', action='store_true',
+                    help='run the long training goldens (trained_<case>.npz) instead')
+    a = ap.parse_intermixed_args()
     if not a.reference:
         ap.error('the path of the reference source tree is required')
     return a
@@ -136,4 +181,7 @@ def _args():
 
 if __name__ == '__main__':
     a = _args()
-    main(a.reference, a.cases)
+    if a.trained:
+        main_trained(a.reference, a.cases)
+    else:
+        main(a.reference, a.cases)

@@ -53,7 +53,7 @@ def test_evaluate_many_equals_one_by_one(name, precision, form):
     # problem's own trainable coefficients keep their initial values, as in the solver)
     for k, net in enumerate(nets):
         prob, _ = O.build_problem(cases.GOLDEN_CASES[name], 'float64')
-        loss64, lossn64, _, _ = O.loss_and_grad(prob, copy.deepcopy(net).double())
+        loss64, lossn64, _, _ = O.loss_and_grad(prob, copy.deepcopy(net).double().cpu())
         assert rel(many[k, 0], loss64) < 1e-5, (k, many[k, 0], loss64)
         assert rel(many[k, 1], lossn64) < 1e-5, (k, many[k, 1], lossn64)
     l0, _ = sol.evaluate(save_graph=False)   # the solver's own network is untouched

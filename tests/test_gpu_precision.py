@@ -1,0 +1,71 @@
+"""Precision study on KdV (u_t + 6 u u_x + u_xxx = 0, 256 x 128 grid, MLP 2-64x4-1, periodic
+u and u_x): the hidden GEMMs in FP32 (CUDA cores), split TF32, TF32 and BF16, each with FP32
+accumulation. For each precision: the loss and gradient relative errors against the reference's
+FP64 evaluation of the same weights, and the solution error at t = 1 against the soliton
+2 sech^2(x - 4t) after the same Adam training from the same seed
+(examples/examples_korteweg_de_vries/example_KdV_periodic.py:22-41 states the solution).
+
+Stated bounds: loss and gradient 1e-5 for FP32 and split TF32 (the FP32 tolerance), 1e-2 for TF32,
+1e-1 for BF16. After training, split TF32 follows the FP32 training closely (its solution within
+1e-2 of FP32's); TF32 and BF16 train to a solution error within 0.05 (absolute, on a relative-L2
+error) of FP32's."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import cases
+from helpers import build_model, golden, rel
+
+STEPS = 3000
+LOSS_GRAD_BOUND = {'fp32': 1e-5, '3xtf32': 1e-5, 'tf32': 1e-2, 'bf16': 1e-1}
+_RESULTS = {}
+
+
+def _soliton_error(model):
+    """Relative L2 error of u(x, t=1) on the grid's last time slice against 2 sech^2(x - 4)."""
+    sol = model.solution_cls
+    grid = sol.grid.to(sol.device)
+    t1 = grid[:, 1] == grid[:, 1].max()
+    pts = grid[t1]
+    with torch.no_grad():
+        u = model.net(pts).double().cpu().numpy()[:, 0]
+    x = pts[:, 0].double().cpu().numpy()
+    exact = 2.0 / np.cosh(x - 4.0) ** 2
+    return rel(u, exact)
+
+
+def _run(precision):
+    if precision in _RESULTS:
+        return _RESULTS[precision]
+    import torch_de_solver_gb300 as T
+    g = golden('kdv_ag')
+    model = build_model(T, 'kdv_ag', weights=g['weights'], precision=precision)
+    loss, _ = model.solution_cls.evaluate()
+    loss.backward()
+    grad = torch.cat([p.grad.reshape(-1) for p in model.net.parameters()]).cpu().numpy()
+    rl, rg = rel(loss.item(), g['loss64']), rel(grad, g['grad64'])
+    e0 = _soliton_error(model)
+    model.train(T.Optimizer('Adam', {'lr': 1e-3}), STEPS + 1)
+    model.solution_cls.check_status()
+    final = model.solution_cls.evaluate(save_graph=False)[0].item()
+    e1 = _soliton_error(model)
+    _RESULTS[precision] = dict(loss_rel=rl, grad_rel=rg, err_init=e0, err=e1, final_loss=final)
+    return _RESULTS[precision]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', ['fp32', '3xtf32', 'tf32', 'bf16'])
+def test_kdv_precision_study(precision):
+    r = _run(precision)
+    ref = _run('fp32')
+    print(f'kdv {precision}: loss rel {r["loss_rel"]:.2e}, grad rel {r["grad_rel"]:.2e} vs FP64; '
+          f'soliton error at t=1: {r["err_init"]:.4f} at init, {r["err"]:.4f} after {STEPS} Adam '
+          f'steps (FP32: {ref["err"]:.4f}); final loss {r["final_loss"]:.5g}')
+    assert r['loss_rel'] < LOSS_GRAD_BOUND[precision] and r['grad_rel'] < LOSS_GRAD_BOUND[precision]
+    assert math.isfinite(r['err']) and r['err'] < r['err_init']
+    if precision == '3xtf32':
+        assert abs(r['err'] - ref['err']) <= 1e-2
+    elif precision != 'fp32':
+        assert abs(r['err'] - ref['err']) <= 0.05

@@ -228,3 +228,31 @@ def test_model_save_uses_the_reference_cache_file_names(tmp_path):
     ck = torch.load(files[0], weights_only=False)
     assert set(ck) == {'model', 'model_state_dict'}
     assert torch.equal(ck['model'][0].weight, m.net[0].weight)
+
+
+def test_shard_ir_splits_residual_rows():
+    """Point sharding of a lowered problem: contiguous residual row ranges per rank (points and
+    per-row coefficients sliced together), loss-slot weights of the whole problem on every rank,
+    boundary groups on rank 0 only."""
+    import torch_de_solver_gb300 as T
+    from torch_de_solver_gb300.prepare import lower, shard_ir, shard_rows
+    d, bc, eq, net, kw = cases.burgers_ag(T, n=10)
+    eq.equation_lst[0]['-mu*d2u/dx2']['coeff'] = lambda g: 0.01 + g[:, 0] ** 2   # per-row array
+    grid = d.build('autograd')
+    bconds = bc.build(d.variable_dict)
+    ir = lower(grid, eq.equation_lst, bconds, 'autograd', 1, 1, d_out=1)
+    res = ir.groups[ir.residual_group]
+    world = 3
+    parts = [shard_ir(ir, r, world) for r in range(world)]
+    assert [shard_rows(res.n_rows, r, world) for r in range(world)] == [(0, 40), (40, 80), (80, 121)]
+    for key in [res.sites[0].points] + [c for c, _, _ in res.terms if isinstance(c, int)]:
+        whole = torch.cat([p.arrays[key] for p in parts])
+        assert torch.equal(whole, ir.arrays[key].reshape(-1))
+    for r, p in enumerate(parts):
+        assert p.slots == ir.slots
+        assert p.groups[p.residual_group].n_rows == shard_rows(res.n_rows, r, world)[1] - \
+            shard_rows(res.n_rows, r, world)[0]
+        assert len(p.groups) == (len(ir.groups) if r == 0 else 1)
+    assert ir.groups[ir.residual_group].n_rows == res.n_rows == 121   # the original is untouched
+    with pytest.raises(ValueError):
+        shard_rows(10, 3, 3)

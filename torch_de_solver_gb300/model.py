@@ -33,8 +33,13 @@ def parameter_registr(model: torch.nn.Module, parameters: dict) -> None:
 
 class Model:
     def __init__(self, net: torch.nn.Module, domain: Domain, equation: Equation,
-                 conditions: Conditions, batch_size: int = None):
+                 conditions: Conditions, batch_size: int = None, shard=None):
+        """shard=(rank, world): one process per GPU, each evaluating its share of the
+        collocation points; the gradient and loss are summed over the ranks of the default
+        torch.distributed group every step (Solution), so every rank takes the same optimizer
+        steps. Not in the reference, which runs on one device."""
         self.net = net
+        self.shard = shard
         self.domain = domain
         self.equation = equation
         self.conditions = conditions
@@ -66,7 +71,7 @@ class Model:
         self.solution_cls = Solution(grid, self.equation.equation_lst, bconds, self.net, mode,
                                      lambda_operator, lambda_bound, h=h, inner_order=inner_order,
                                      boundary_order=boundary_order, precision=precision, form=form,
-                                     tol=tol, batch_size=self.batch_size)
+                                     tol=tol, batch_size=self.batch_size, shard=self.shard)
         self.net = self.solution_cls.model
         self._graph = None
 
@@ -132,8 +137,10 @@ class Model:
             cbs.on_epoch_begin()
             self.optimizer.zero_grad()
             for _ in range(steps):
-                if fused:   # mini-batch steps change their inputs on the host: no graph
-                    loss = self._fused_step(capture=(n_eager == 2 and batches is None))
+                if fused:   # mini-batch steps change their inputs on the host, sharded steps
+                    # exchange through torch.distributed between launches: no graph for either
+                    loss = self._fused_step(capture=(n_eager == 2 and batches is None
+                                                     and self.shard is None))
                     n_eager += 1
                     self.cur_loss = loss.clone() if cbs.callbacks else loss
                 else:

@@ -602,3 +602,50 @@ def lower(grid, operator, bconds, mode, lambda_operator, lambda_bound, h=0.001, 
         for gi, _ in ir.bc_parts[t]:
             ir.groups[gi].slot_first = slot
     return ir
+
+
+def shard_rows(n, rank, world):
+    """Rows [r0, r1) of `n` residual rows that rank `rank` of `world` evaluates: contiguous
+    ranges whose sizes differ by at most one, in rank order."""
+    if not 0 <= rank < world:
+        raise ValueError(f'rank {rank} outside a world of {world}')
+    return n * rank // world, n * (rank + 1) // world
+
+
+def shard_ir(ir, rank, world):
+    """The part of a lowered problem that rank `rank` of `world` evaluates when the collocation
+    points are split across devices: the residual group keeps rows [r0, r1) (its points,
+    per-row coefficients and per-row weights sliced to them) and only rank 0 keeps the boundary
+    groups. The loss-slot weights are the unsharded problem's (lambda over the global point
+    count, tedeous/losses.py:58), so the per-rank losses and gradients add up to the unsharded
+    ones: the residual is independent per point and the loss is a sum over points. The op / bval
+    fields of a rank describe its own rows only."""
+    import copy as _copy
+    if ir.causal is not None:
+        raise NotImplementedError('the causal loss couples every time slice across the points: '
+                                  'it is not sharded')
+    res = ir.groups[ir.residual_group]
+    r0, r1 = shard_rows(res.n_rows, rank, world)
+    out = _copy.copy(ir)
+    out.arrays = list(ir.arrays)
+    keys = {s.points for s in res.sites}
+    keys |= {c for c, _, _ in res.terms if isinstance(c, int)}
+    if res.row_weight is not None:
+        keys.add(res.row_weight)
+    if res.target is not None:
+        keys.add(res.target)
+    for k in keys:
+        a = ir.arrays[k]
+        per_row = a.numel() // res.n_rows
+        out.arrays[k] = a.reshape(res.n_rows, per_row)[r0:r1].reshape(-1).contiguous()
+    new_res = _copy.copy(res)
+    new_res.n_rows = r1 - r0
+    if rank == 0:
+        out.groups = [new_res if i == ir.residual_group else g for i, g in enumerate(ir.groups)]
+    else:
+        out.groups = [new_res]
+        out.residual_group = 0
+        out.bc_parts = {t: [] for t in ir.bc_types}
+    out.n_residual_rows = r1 - r0
+    out.shard = (rank, world, r0, r1)
+    return out

@@ -16,7 +16,7 @@ import ctypes
 import torch
 
 from . import _lib
-from .prepare import CoeffParam, lower
+from .prepare import CoeffParam, lower, shard_ir
 
 
 def default_precision(precision, form):
@@ -218,6 +218,19 @@ class DevicePlan:
             None if outputs is None else outputs.data_ptr(), s.cuda_stream), 'tdg_loss')
 
 
+def allreduce_sum(*tensors):
+    """Sum each tensor over the ranks of the default torch.distributed process group (NCCL
+    between GPUs, gloo on CPU), in place; nothing without an initialised group of more than one
+    rank. The one exchange of a point-sharded step: the flat parameter gradient and the FP64
+    (loss, loss_normalized) partials."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return
+    for t in tensors:
+        if t is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.SUM)
+
+
 class _FusedLoss(torch.autograd.Function):
     """(loss, loss_normalized) of the current parameters; the gradient is computed in the same
     fused launch and returned, scaled by the incoming gradient, in backward()."""
@@ -288,11 +301,15 @@ class Solution:
     tdg_causal_weights turns it into per-row weights, then the loss and gradient launch applies
     them. batch_size selects mini-batches of the collocation points: in 'autograd' mode each
     evaluation gathers the batch's points (and per-point coefficients) with tdg_gather_rows into
-    a plan made for that batch size; 'NN' terms ignore the batch, as the reference's do."""
+    a plan made for that batch size; 'NN' terms ignore the batch, as the reference's do.
+    shard=(rank, world) evaluates this rank's contiguous share of the residual rows (rank 0 also
+    the boundary conditions, prepare.shard_ir) and sums the gradient and the loss over the ranks
+    of the default torch.distributed group after every launch (allreduce_sum); without an
+    initialised group the per-rank parts are returned as they are."""
 
     def __init__(self, grid, operator, bconds, model, mode, lambda_operator, lambda_bound,
                  h=0.001, inner_order='1', boundary_order='2', precision=None, form='fused',
-                 device=None, tol=0, batch_size=None):
+                 device=None, tol=0, batch_size=None, shard=None):
         if not torch.cuda.is_available():
             raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
         self.device = torch.device('cuda', torch.cuda.current_device()) if device is None \
@@ -308,6 +325,12 @@ class Solution:
         args = (operator, bconds, mode, lambda_operator, lambda_bound, h, inner_order,
                 boundary_order)
         self.ir = lower(grid, *args, d_out=widths[-1], tol=tol)
+        self.shard = None
+        if shard is not None:
+            if batch_size is not None:
+                raise NotImplementedError('mini-batches of a point-sharded problem')
+            self.shard = tuple(shard)
+            self.ir = shard_ir(self.ir, *self.shard)
         self.model = model.to(self.device)
         self.params = device_parameters(self.model, self.ir.coeff_params)
         self.flat = flatten_parameters(self.params, self.device)
@@ -436,6 +459,8 @@ class Solution:
             self.plan.loss_grad(self.flat, self._grad, self._loss_buf, self._outputs)
         else:
             self.plan.loss(self.flat, self._loss_buf, self._outputs)
+        if self.shard is not None:   # this rank's rows -> the whole problem's loss and gradient
+            allreduce_sum(self._grad if with_grad else None, self._loss_buf)
 
     def evaluate(self, save_graph: bool = True):
         """(loss, loss_normalized), each of shape (1,) like the reference's."""
@@ -523,7 +548,7 @@ class Solution:
             if true:
                 v = torch.cat([x.reshape(-1) for x in ir.bc_true[t]]).to(self.device)
             else:
-                pieces = []
+                pieces = [torch.zeros(0, device=self.device)]   # no pieces on a shard > 0
                 for gi, n in ir.bc_parts[t]:
                     off = self.plan.group_out[0][gi]
                     pieces.append(self._outputs[off:off + n])
