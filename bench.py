@@ -62,6 +62,8 @@ def parse():
     ap.add_argument('--no-compare', action='store_true',
                     help='skip the plain-form and ATen timings of the same workload')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-autotune', action='store_true',
+                    help='sweep: keep the default tile schedule instead of the autotuned one')
     ap.add_argument('--optimizer', default='adam', choices=['adam', 'lbfgs'],
                     help='lbfgs: time L-BFGS iterations (device history, FP64 dots, strong-Wolfe '
                          'line search) instead of Adam steps')
@@ -268,6 +270,37 @@ def read_traffic(tag):
     return None
 
 
+def sequential_sweep_ms(args, form, precision, steps):
+    """The reference's way of running the sweep on the GPU: one Model per solve, trained one after
+    another (tedeous/model.py:134-195 has no batched API). Each solve's step (loss+gradient
+    launch(es), Adam) is timed over `steps` steps after one warm-up with CUDA events; the sum over
+    the solves is the time of one sweep step."""
+    import torch
+    import torch_de_solver_gb300 as T
+    total = 0.0
+    for b in sweep_builders(WORKLOADS['sweep'][1]['n_solves']):
+        d, bc, eq, net, kw = b(T)
+        kw = dict(kw)
+        model = T.Model(net, d, eq, bc)
+        model.compile(kw.pop('mode'), precision=precision, form=form, **kw)
+        sol = model.solution_cls
+        opt = T.Optimizer('Adam', {'lr': 1e-3}).optimizer_choice(model.mode, model.net)
+
+        def step():
+            sol.plan.loss_grad(sol.flat, sol._grad, sol._loss_buf, sol._outputs)
+            opt.apply(sol._grad)
+        step()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            step()
+        e.record()
+        torch.cuda.synchronize()
+        total += a.elapsed_time(e) / steps
+        del model, sol, opt
+    return total
+
+
 def run_sweep(args, world):
     """256 solves of u_t = a u_xx + b u u_x + c u in one loss+gradient launch per step, one
     batched Adam launch, against 256 separate solves on the CPU sample."""
@@ -282,7 +315,8 @@ def run_sweep(args, world):
         d, bc, eq, net, kw = b(T)
         models.append(T.Model(net, d, eq, bc))
     bm = T.BatchedModel(models)
-    bm.compile('autograd', lambda_operator=1, lambda_bound=1, precision=args.precision)
+    bm.compile('autograd', lambda_operator=1, lambda_bound=1, precision=args.precision,
+               autotune=not args.no_autotune)
     n_pts = sum(ir.n_residual_rows for ir in bm.irs)
     flush = torch.empty(2 * L2_BYTES // 4, device=dev)
     stream = torch.cuda.current_stream(dev)
@@ -332,14 +366,26 @@ def run_sweep(args, world):
     peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
     peak = peaks.get('bf16_tflops', 1900.0) / 2.0
     achieved = flops / (ms / 1e3) / 1e12
+    seq = {}
+    if not args.no_compare:
+        k = max(1, min(args.steps, 5))
+        seq = {'sequential_plain_ms_per_step': round(sequential_sweep_ms(args, 'plain', 'fp32', k), 3),
+               'sequential_fused_ms_per_step': round(sequential_sweep_ms(args, 'fused', args.precision, k), 3)}
+        seq['batched_vs_sequential_plain'] = round(seq['sequential_plain_ms_per_step'] / ms, 2)
+        seq['batched_vs_sequential_fused'] = round(seq['sequential_fused_ms_per_step'] / ms, 2)
     return {'metric': METRIC, 'value': round(world * n_pts / (ms / 1e3), 1), 'unit': UNIT,
             'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
-            'ms_per_step': round(ms, 4), 'steps_per_s': round(1e3 / ms, 3),
+            'ms_per_step': round(ms, 4), 'steps_per_s': round(1e3 / ms, 3), **seq,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic (seeded coefficients, grids and networks)',
             'config': {'workload': WORKLOADS['sweep'][3], 'solves': n_solves,
                        'collocation_points': n_pts, 'precision': args.precision,
                        'form': 'fused, one launch for all solves', 'optimizer': 'Adam lr=1e-3',
+                       'schedule': bm.plan.schedule or 'default',
+                       'autotune': None if bm.tuning is None else {
+                           'default_launch_ms': bm.tuning['default_ms'],
+                           'chosen_launch_ms': bm.tuning['ms'],
+                           'trials': [(t['schedule'], t['ms']) for t in bm.tuning['trials']]},
                        'l2': 'flushed between timed steps (256 MiB write)',
                        'parallelism': f'replicas x{world}'},
             'e2e': {'value': round(world * n_pts / e2e_sec, 1), 'unit': UNIT,

@@ -203,6 +203,24 @@ int32_t tdg_site_class(int32_t n_streams, const tdg_stream_desc* streams);
 
 /* Validate the description, build tile schedules and device tables, allocate the workspace. */
 tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** plan);
+
+/* How a plan cuts its rows into tiles and spreads the tiles over persistent CTAs; the knobs the
+ * autotuner (torch_de_solver_gb300.autotune) searches for a problem shape. max_rows caps the
+ * (stream, point) rows of a tile (a multiple of 32, at most 128): a group of S streams runs
+ * floor(max_rows / S) points per tile. n_ctas is the number of persistent CTAs (0: one per SM;
+ * at most the SM count). balance 0 gives every CTA an equal number of consecutive tiles, balance 1
+ * an equal share of estimated work (a fixed cost per tile plus its filled rows). */
+typedef struct {
+  int32_t max_rows;
+  int32_t n_ctas;
+  int32_t balance;
+  int32_t reserved;
+} tdg_schedule;
+/* tdg_plan_create with a schedule (NULL: {128, 0, 0}, the tdg_plan_create default). Same
+ * replacement as tdg_plan_create (tedeous/solution.py:23-88): no counterpart of the schedule in
+ * the reference, which evaluates every point set in one batch. */
+tdg_status tdg_plan_create_scheduled(const tdg_problem_desc* desc, const tdg_schedule* schedule,
+                                     tdg_plan** plan);
 tdg_status tdg_plan_destroy(tdg_plan* plan);
 tdg_status tdg_plan_get_info(const tdg_plan* plan, tdg_plan_info* info);
 /* Replace the device pointer of array `index` (same length), e.g. freshly copied points. */

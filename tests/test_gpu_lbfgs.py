@@ -36,7 +36,7 @@ def test_direction_matches_fp64_two_loop_with_wraparound_and_rejections():
     _lib.check(lib.tdg_lbfgs_create(n, hist, ctypes.byref(h)), 'create')
     stream = torch.cuda.current_stream().cuda_stream
     gen = torch.Generator().manual_seed(5)
-    pairs, h_diag, n_push = [], 1.0, 0
+    pairs, h_diag, n_push, accepted, rejected = [], 1.0, 0, 0, 0
     g_prev = torch.randn(n, generator=gen)
     d_prev = torch.randn(n, generator=gen)
     try:
@@ -57,6 +57,9 @@ def test_direction_matches_fp64_two_loop_with_wraparound_and_rejections():
                     pairs.pop(0)
                 pairs.append((s, y, 1.0 / ys))
                 h_diag = ys / float(y @ y)
+                accepted += 1
+            else:
+                rejected += 1
             out = torch.empty(n, device='cuda')
             _lib.check(lib.tdg_lbfgs_direction(h, gd.data_ptr(), out.data_ptr(),
                                                min(n_push, hist), stream), 'direction')
@@ -64,7 +67,8 @@ def test_direction_matches_fp64_two_loop_with_wraparound_and_rejections():
             got = out.double().cpu()
             assert rel(got.numpy(), want.numpy()) < 1e-6, (it, rel(got.numpy(), want.numpy()))
             g_prev, d_prev = g, out.cpu()
-        assert len(pairs) == hist
+        # the run covered both a full ring that wrapped around and rejected pairs
+        assert accepted > hist and rejected >= 2, (accepted, rejected)
     finally:
         lib.tdg_lbfgs_destroy(h)
 

@@ -6,9 +6,12 @@ FP64 evaluation of the same weights, and the solution error at t = 1 against the
 (examples/examples_korteweg_de_vries/example_KdV_periodic.py:22-41 states the solution).
 
 Stated bounds: loss and gradient 1e-5 for FP32 and split TF32 (the FP32 tolerance), 1e-2 for TF32,
-1e-1 for BF16. After training, split TF32 follows the FP32 training closely (its solution within
-1e-2 of FP32's); TF32 and BF16 train to a solution error within 0.05 (absolute, on a relative-L2
-error) of FP32's."""
+1e-1 for BF16. After 3000 Adam steps from the same weights every precision trains to a soliton
+error within 0.03 (absolute, on a relative-L2 error) of the FP32 run's. Measured on a GB300: loss /
+gradient errors 4.8e-7 / 1.6e-7 (FP32), 4.4e-8 / 2.6e-6 (split TF32), 2.3e-5 / 2.6e-4 (TF32),
+2.9e-4 / 2.4e-3 (BF16); soliton error at t = 1 from 1.214 at initialisation to 0.0580 (FP32),
+0.0661 (split TF32), 0.0671 (TF32), 0.0629 (BF16). The trainings separate through the rounding
+of thousands of Adam steps, so the solution bound is looser than the per-evaluation one."""
 import math
 
 import numpy as np
@@ -65,7 +68,5 @@ def test_kdv_precision_study(precision):
           f'steps (FP32: {ref["err"]:.4f}); final loss {r["final_loss"]:.5g}')
     assert r['loss_rel'] < LOSS_GRAD_BOUND[precision] and r['grad_rel'] < LOSS_GRAD_BOUND[precision]
     assert math.isfinite(r['err']) and r['err'] < r['err_init']
-    if precision == '3xtf32':
-        assert abs(r['err'] - ref['err']) <= 1e-2
-    elif precision != 'fp32':
-        assert abs(r['err'] - ref['err']) <= 0.05
+    if precision != 'fp32':
+        assert abs(r['err'] - ref['err']) <= 0.03

@@ -48,7 +48,8 @@ def test_trained_solution_matches_the_reference_training(name, precision):
     curve_drift = float(np.max(np.abs(ours[:, 1] - ref_curve[:, 1]) / np.abs(ref_curve[:, 1])))
     msg = (f'{name} {precision} {epochs} epochs: |u - u_ref| / |u_ref| = {drift:.2e}, loss curve '
            f'max rel gap {curve_drift:.2e}, final loss {ours[-1, 1]:.6g} (reference '
-           f'{ref_curve[-1, 1]:.6g})')
+           f'{ref_curve[-1, 1]:.6g}); curves (epoch, ours, reference): '
+           f'{[(int(a), float(b), float(c)) for a, b, c in zip(ours[:, 0], ours[:, 1], ref_curve[:, 1])]}')
     if name == 'heat_nn':
         x, t = g['grid'][:, 0], g['grid'][:, 1]
         exact = np.exp(-math.pi ** 2 * t) * np.sin(math.pi * x)

@@ -69,3 +69,16 @@ def test_lbfgs_entry_points_validate_on_the_host():
     assert lib.tdg_lbfgs_stats(None, None, None, None, None, None) == _lib.ERR_INVALID
     assert lib.tdg_axpy(None, None, 1.0, None, 3, None) == _lib.ERR_INVALID
     assert lib.tdg_lbfgs_destroy(None) == _lib.OK
+
+
+def test_schedule_is_validated_before_the_description():
+    """tdg_plan_create_scheduled rejects a malformed tile schedule on the host."""
+    from torch_de_solver_gb300 import _lib
+    lib = _lib.load()
+    desc = _lib.ProblemDesc()
+    h = ctypes.c_void_p()
+    for bad in ((100, 0, 0, 0), (160, 0, 0, 0), (16, 0, 0, 0), (128, -1, 0, 0), (128, 0, 2, 0)):
+        sc = _lib.Schedule(*bad)
+        assert lib.tdg_plan_create_scheduled(ctypes.byref(desc), ctypes.byref(sc),
+                                             ctypes.byref(h)) == _lib.ERR_INVALID, bad
+        assert b'schedule' in lib.tdg_last_error()

@@ -83,6 +83,10 @@ class PlanInfo(ctypes.Structure):
                 ('flops_total', f64)]
 
 
+class Schedule(ctypes.Structure):
+    _fields_ = [('max_rows', i32), ('n_ctas', i32), ('balance', i32), ('reserved', i32)]
+
+
 class AdamDesc(ctypes.Structure):
     _fields_ = [('lr', f32), ('beta1', f32), ('beta2', f32), ('eps', f32), ('weight_decay', f32),
                 ('maximize', i32)]
@@ -95,6 +99,8 @@ SIGNATURES = {
     'tdg_launch_count': (i64, []),
     'tdg_site_class': (i32, [i32, ctypes.POINTER(StreamDesc)]),
     'tdg_plan_create': (i32, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(vp)]),
+    'tdg_plan_create_scheduled': (i32, [ctypes.POINTER(ProblemDesc), ctypes.POINTER(Schedule),
+                                        ctypes.POINTER(vp)]),
     'tdg_plan_destroy': (i32, [vp]),
     'tdg_plan_get_info': (i32, [vp, ctypes.POINTER(PlanInfo)]),
     'tdg_plan_set_array': (i32, [vp, i32, vp, i64]),

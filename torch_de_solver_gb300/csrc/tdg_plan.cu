@@ -8,8 +8,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
+
+#include <cudaTypedefs.h>
 
 #include "tdg_internal.h"
 #include "tdg_jetcls.h"
@@ -87,12 +90,32 @@ struct tdg_plan {
   float* d_gy = nullptr;
   double* d_slot_sum = nullptr;
   int64_t wpack_fwd[TDG_MAX_LAYERS] = {0}, wpack_bwd[TDG_MAX_LAYERS] = {0};
+  CUtensorMap dw_map[TDG_MAX_LAYERS];   // TMA maps of the hidden dW over the gradient segments
+  bool tma_flush = false;
   int64_t wpack_stride = 0;
   int64_t workspace_bytes = 0;
   bool arrays_dirty = false;
 };
 
 namespace {
+
+// cuTensorMapEncodeTiled of the driver, looked up once through the runtime (no libcuda link);
+// null when unavailable
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::mutex mu;
+  static bool looked = false;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!looked) {
+    looked = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }
+  return fn;
+}
 
 using Key = std::vector<int>;   // sorted axes of a derivative stream
 
@@ -178,7 +201,7 @@ int site_class(const DevGroup& G, const std::vector<Key>& keys, int base, int ns
 }
 
 tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d_in, int d_out,
-                       bool tables_only, DevGroup& G, int& S_out) {
+                       bool tables_only, int max_rows, DevGroup& G, int& S_out) {
   memset(&G, 0, sizeof(G));
   if (g.n_sites < 1 || g.n_sites > MAX_SITES) return fail(TDG_ERR_UNSUPPORTED, "group has %d sites (1..%d)", g.n_sites, MAX_SITES);
   if (g.site_first < 0 || g.site_first + g.n_sites > d.n_sites) return fail(TDG_ERR_INVALID, "site range out of bounds");
@@ -346,7 +369,7 @@ tdg_status build_group(const tdg_problem_desc& d, const tdg_group_desc& g, int d
   }
   G.n_rows = g.n_rows;
   G.S = S;
-  G.T = RMAX / S;
+  G.T = max_rows / S;
   G.n_sites = g.n_sites;
   G.n_outputs = g.n_outputs;
   G.n_terms = g.n_terms;
@@ -382,7 +405,20 @@ int32_t tdg_site_class(int32_t n_streams, const tdg_stream_desc* streams) {
 }
 
 tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
+  return tdg_plan_create_scheduled(desc, nullptr, out);
+}
+
+tdg_status tdg_plan_create_scheduled(const tdg_problem_desc* desc, const tdg_schedule* sched,
+                                     tdg_plan** out) {
   if (!desc || !out) return fail(TDG_ERR_INVALID, "null argument");
+  tdg_schedule sc{RMAX, 0, 0, 0};
+  if (sched) {
+    sc = *sched;
+    if (sc.max_rows < 32 || sc.max_rows > RMAX || sc.max_rows % 32)
+      return fail(TDG_ERR_INVALID, "schedule max_rows %d (a multiple of 32, 32..%d)", sc.max_rows, RMAX);
+    if (sc.n_ctas < 0) return fail(TDG_ERR_INVALID, "schedule n_ctas %d < 0", sc.n_ctas);
+    if (sc.balance < 0 || sc.balance > 1) return fail(TDG_ERR_INVALID, "schedule balance %d (0 or 1)", sc.balance);
+  }
   *out = nullptr;
   const tdg_problem_desc& d = *desc;
   const int L = d.mlp.n_layers;
@@ -446,11 +482,15 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     const tdg_group_desc& g = d.groups[gi];
     if (g.problem < 0 || g.problem >= d.n_problems) { free_plan(p); return fail(TDG_ERR_INVALID, "group problem out of range"); }
     int S = 0;
-    tdg_status st = build_group(d, g, d_in, d_out, tables_only, groups[gi], S);
+    tdg_status st = build_group(d, g, d_in, d_out, tables_only, sc.max_rows, groups[gi], S);
     if (st != TDG_OK) { free_plan(p); return st; }
+    if (sc.max_rows / S < 1) {
+      free_plan(p);
+      return fail(TDG_ERR_INVALID, "schedule max_rows %d holds no point of a %d-stream group", sc.max_rows, S);
+    }
     p->max_streams = std::max(p->max_streams, S);
     p->ginfo.push_back(HostGroupInfo{g.n_rows, S, g.problem});
-    const int T = RMAX / S;
+    const int T = sc.max_rows / S;
     for (int r0 = 0; r0 < g.n_rows; r0 += T)
       tiles.push_back(DevTile{gi, r0, std::min(T, g.n_rows - r0), 0, 0, g.problem, {0, 0}});
     p->flops_hidden += 3.0 * 2.0 * (double)g.n_rows * S * hidden_pairs;
@@ -468,14 +508,34 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
     for (int c = 1; c < jetcls::N_CLASSES; ++c)
       if (rows_of_class[c] > rows_of_class[p->cls_main]) p->cls_main = c;
   }
-  // contiguous equal-count partition of the tile list over one CTA per SM
+  // contiguous partition of the tile list (in group order) over the persistent CTAs, one per SM
+  // by default: equal tile counts, or (balance 1) equal estimated work, each tile weighing a fixed
+  // share for its layer-by-layer synchronisation plus its filled (stream, point) rows
   int sms = 0;
   ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
   if (ce != cudaSuccess) { free_plan(p); return cuda_fail(ce, "cudaDeviceGetAttribute"); }
   const int n_tiles = (int)tiles.size();
-  const int n_ctas = std::max(1, std::min(n_tiles, sms));
+  const int max_ctas = sc.n_ctas > 0 ? std::min(sc.n_ctas, sms) : sms;
+  const int n_ctas = std::max(1, std::min(n_tiles, max_ctas));
   std::vector<int32_t> cta_begin(n_ctas + 1);
-  for (int c = 0; c <= n_ctas; ++c) cta_begin[c] = (int32_t)((int64_t)n_tiles * c / n_ctas);
+  if (sc.balance == 0) {
+    for (int c = 0; c <= n_ctas; ++c) cta_begin[c] = (int32_t)((int64_t)n_tiles * c / n_ctas);
+  } else {
+    std::vector<double> prefix(n_tiles + 1, 0.0);
+    for (int t = 0; t < n_tiles; ++t)
+      prefix[t + 1] = prefix[t] + 1.0 + (double)tiles[t].nvalid * groups[tiles[t].group].S / RMAX;
+    cta_begin[0] = 0;
+    int t = 0;
+    for (int c = 1; c < n_ctas; ++c) {
+      const double target = prefix[n_tiles] * c / n_ctas;
+      while (t < n_tiles && prefix[t + 1] <= target) ++t;
+      // at least one tile per CTA before and after this cut
+      t = std::max(t, (int)cta_begin[c - 1] + 1);
+      t = std::min(t, n_tiles - (n_ctas - c));
+      cta_begin[c] = t;
+    }
+    cta_begin[n_ctas] = n_tiles;
+  }
   // segments: one per (CTA, problem) pair, in CTA order
   std::vector<std::vector<int32_t>> segs_of(d.n_problems);
   int n_seg = 0;
@@ -557,6 +617,24 @@ tdg_status tdg_plan_create(const tdg_problem_desc* desc, tdg_plan** out) {
       off += np * kp * es;
     }
     p->wpack_stride = off;   // every problem has its own weights
+    // the hidden dW flush as TMA tensor reductions: dW_j ([width j+1][width j] floats, rows of
+    // width j) of every gradient segment as one 3D tensor, 128-byte swizzled [N][32] boxes.
+    // TDG_TMA_FLUSH=0 keeps the vector-atomic flush (an A/B switch; both give the same sums).
+    const char* tf = std::getenv("TDG_TMA_FLUSH");
+    PFN_cuTensorMapEncodeTiled_v12000 enc = (tf && tf[0] == '0') ? nullptr : tensor_map_encoder();
+    p->tma_flush = enc != nullptr && d.form == TDG_FORM_FUSED && L > 2;
+    for (int j = 1; p->tma_flush && j < L - 1; ++j) {
+      const cuuint64_t K = (cuuint64_t)d.mlp.width[j], N = (cuuint64_t)d.mlp.width[j + 1];
+      const cuuint64_t dims[3] = {K, N, (cuuint64_t)p->n_segments};
+      const cuuint64_t strides[2] = {K * sizeof(float), (cuuint64_t)p->part_stride * sizeof(float)};
+      const cuuint32_t box[3] = {32, (cuuint32_t)N, 1};
+      const cuuint32_t elem[3] = {1, 1, 1};
+      const CUresult r = enc(&p->dw_map[j], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, p->d_partial + p->w_off[j],
+                             dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) p->tma_flush = false;   // the atomic flush stays available
+    }
     if ((st = dev_alloc(p, (void**)&p->d_wpack, (size_t)std::max<int64_t>(off * d.n_problems, 16)))) {
       free_plan(p);
       return st;
@@ -667,6 +745,8 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
     }
     for (int l = 0; l <= p->n_layers; ++l) t.width[l] = p->width[l];
     t.err = p->d_err;
+    t.dw_map = p->dw_map;
+    t.tma_flush = p->tma_flush;
     if (do_grad) {   // the tensor-core kernel accumulates hidden dW with atomic adds
       e = cudaMemsetAsync(p->d_partial, 0, sizeof(float) * p->part_stride * p->n_segments, s);
       if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");

@@ -52,11 +52,13 @@ class Model:
                 lambda_bound: Union[List[float], float], normalized_loss_stop: bool = False,
                 h: float = 0.001, inner_order: str = '1', boundary_order: str = '2',
                 derivative_points: int = 2, weak_form: List[callable] = None, tol: float = 0,
-                removed_domains: list = None, precision: str = None, form: str = 'fused'):
+                removed_domains: list = None, precision: str = None, form: str = 'fused',
+                autotune: bool = False):
         """Arguments as in tedeous/model.py:56-113, plus precision and form ('fused' or 'plain').
         precision: '3xtf32' (split-TF32 tensor cores at FP32 tolerance; the default of the fused
         form), 'fp32' (CUDA cores, bitwise reproducible gradient; the plain form's only one),
-        'tf32' or 'bf16'."""
+        'tf32' or 'bf16'. autotune=True picks the fused kernel's tile schedule by timing
+        candidates on the device (torch_de_solver_gb300.autotune)."""
         if weak_form:
             raise NotImplementedError('weak-form losses are not implemented on the device path')
         self.mode = mode
@@ -71,7 +73,8 @@ class Model:
         self.solution_cls = Solution(grid, self.equation.equation_lst, bconds, self.net, mode,
                                      lambda_operator, lambda_bound, h=h, inner_order=inner_order,
                                      boundary_order=boundary_order, precision=precision, form=form,
-                                     tol=tol, batch_size=self.batch_size, shard=self.shard)
+                                     tol=tol, batch_size=self.batch_size, shard=self.shard,
+                                     autotune=autotune)
         self.net = self.solution_cls.model
         self._graph = None
 
@@ -171,7 +174,11 @@ class BatchedModel:
         self.models = list(models)
 
     def compile(self, mode: str, lambda_operator, lambda_bound, h: float = 0.001,
-                inner_order: str = '1', boundary_order: str = '2', precision: str = None):
+                inner_order: str = '1', boundary_order: str = '2', precision: str = None,
+                autotune: bool = False):
+        """autotune=True picks the tile schedule of the batched launch by timing candidates on
+        the device (torch_de_solver_gb300.autotune, cached per problem shape and GPU);
+        self.tuning then holds the search record."""
         from .prepare import lower
         from .solution import (DevicePlan, default_precision, device_parameters,
                                flatten_parameters, mlp_widths)
@@ -189,7 +196,12 @@ class BatchedModel:
                              lambda_bound, h, inner_order, boundary_order, d_out=widths[-1]))
         self.mode = mode
         self.irs = irs
-        self.plan = DevicePlan(irs, widths, dev, default_precision(precision, 'fused'))
+        prec = default_precision(precision, 'fused')
+        schedule, self.tuning = None, None
+        if autotune:
+            from .autotune import tune
+            schedule, self.tuning = tune(irs, widths, dev, prec)
+        self.plan = DevicePlan(irs, widths, dev, prec, schedule=schedule)
         P = self.plan.n_params
         for m in self.models:
             m.net.to(dev)

@@ -90,7 +90,9 @@ def params_are_views(params, flat):
 class DevicePlan:
     """A tdg_plan for one or more lowered problems (ProblemIR) sharing one MLP shape."""
 
-    def __init__(self, irs, widths, device, precision='fp32', form='fused'):
+    def __init__(self, irs, widths, device, precision='fp32', form='fused', schedule=None):
+        """schedule: None for the default tile schedule, or a dict (max_rows, n_ctas, balance)
+        as torch_de_solver_gb300.autotune finds (tdg_plan_create_scheduled)."""
         if precision not in _lib.PREC:
             raise ValueError(f'precision {precision!r}')
         if form not in _lib.FORM:
@@ -183,9 +185,17 @@ class DevicePlan:
             k['parts'], len(slots), k['slots'], len(self.arrays), k['ptrs'], k['lens'],
             _lib.PREC[precision], _lib.FORM[form], self.n_coeff)
         handle = ctypes.c_void_p()
+        self.schedule = None if schedule is None else dict(schedule)
         with torch.cuda.device(device):
-            _lib.check(lib.tdg_plan_create(ctypes.byref(desc), ctypes.byref(handle)),
-                       'tdg_plan_create')
+            if schedule is None:
+                _lib.check(lib.tdg_plan_create(ctypes.byref(desc), ctypes.byref(handle)),
+                           'tdg_plan_create')
+            else:
+                sc = _lib.Schedule(int(schedule.get('max_rows', 128)),
+                                   int(schedule.get('n_ctas', 0)), int(schedule.get('balance', 0)), 0)
+                _lib.check(lib.tdg_plan_create_scheduled(ctypes.byref(desc), ctypes.byref(sc),
+                                                         ctypes.byref(handle)),
+                           'tdg_plan_create_scheduled')
         self.handle = handle
         info = _lib.PlanInfo()
         _lib.check(lib.tdg_plan_get_info(handle, ctypes.byref(info)), 'tdg_plan_get_info')
@@ -305,11 +315,13 @@ class Solution:
     shard=(rank, world) evaluates this rank's contiguous share of the residual rows (rank 0 also
     the boundary conditions, prepare.shard_ir) and sums the gradient and the loss over the ranks
     of the default torch.distributed group after every launch (allreduce_sum); without an
-    initialised group the per-rank parts are returned as they are."""
+    initialised group the per-rank parts are returned as they are. autotune=True times the
+    candidate tile schedules of torch_de_solver_gb300.autotune on this problem (cached per shape
+    and GPU) and builds the plans with the fastest."""
 
     def __init__(self, grid, operator, bconds, model, mode, lambda_operator, lambda_bound,
                  h=0.001, inner_order='1', boundary_order='2', precision=None, form='fused',
-                 device=None, tol=0, batch_size=None, shard=None):
+                 device=None, tol=0, batch_size=None, shard=None, autotune=False):
         if not torch.cuda.is_available():
             raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
         self.device = torch.device('cuda', torch.cuda.current_device()) if device is None \
@@ -357,6 +369,10 @@ class Solution:
         else:
             self._irs[self.ir.groups[self.ir.residual_group].n_rows] = (self.ir, [])
         self._loss_buf = torch.zeros(2, device=self.device, dtype=torch.float64)
+        self.schedule, self.tuning = None, None
+        if autotune and self.form == 'fused':
+            from .autotune import tune
+            self.schedule, self.tuning = tune([self.ir], widths, self.device, self.precision)
         self._build_plans(widths)
         self._clone_grad = True
         self.bval_keys = list(self.ir.bc_types)
@@ -368,7 +384,8 @@ class Solution:
         self._plans = {}
         n_grid = self.grid.shape[0]
         for n, (ir, keys) in self._irs.items():
-            plan = DevicePlan([ir], widths, self.device, self.precision, self.form)
+            plan = DevicePlan([ir], widths, self.device, self.precision, self.form,
+                              schedule=getattr(self, 'schedule', None))
             gathers = [(plan.arrays[plan.array_maps[0][kb]], self._row_src[kf],
                         self._full_ir.arrays[kf].numel() // n_grid) for kb, kf in keys]
             self._plans[n] = (ir, plan, gathers)
