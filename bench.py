@@ -7,13 +7,19 @@ output. Synthetic, seeded inputs: the grid and the closed-form boundary values a
 the network is seeded torch default init.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload kovasznay|burgers|kdv|heat] [--points-per-axis n]
+                  [--workload kovasznay|burgers|kdv|heat|sweep] [--points-per-axis n]
+                  [--precision 3xtf32|fp32|tf32|bf16] [--form fused|plain]
+                  [--optimizer adam|lbfgs] [--no-compare] [--no-cpu-baseline] [--no-autotune]
 
 Our arm prints one JSON line with the device-resident throughput (value), the end-to-end
-throughput through the public API with host buffers (e2e), the roofline of the fused kernel, a
-CPU baseline (the oracle's restatement of the reference algorithm, timed on the host cores on a
-bounded sample), sampled GPU clocks and the number of library kernel launches. --impl reference
-times that CPU restatement alone on the same workload family.
+throughput through the public API with host buffers (e2e), the roofline of the fused kernel, the
+plain form on the same workload (plain_ms_per_step, fused_vs_plain), the reference's operation
+sequence through ATen/cuBLAS on the GPU (aten_reference), a CPU baseline (the oracle's
+restatement of the reference algorithm on the host cores, on a bounded sample), sampled GPU clocks
+and the number of library kernel launches. --optimizer lbfgs times L-BFGS iterations instead;
+--workload sweep times the 256-solve batched sweep with its autotuned schedule against 256
+sequential solves. --impl reference times the CPU restatement alone on the same workload family,
+honouring --steps and --warmup.
 """
 
 import argparse

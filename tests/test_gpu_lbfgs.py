@@ -42,7 +42,9 @@ def test_direction_matches_fp64_two_loop_with_wraparound_and_rejections():
     try:
         for it in range(8):
             t = 0.5 + 0.1 * it
-            g = g_prev + 0.3 * torch.randn(n, generator=gen)
+            # y = c * s with c in [0.5, 1.5) plus a little noise: positive curvature, accepted
+            c = 0.5 + torch.rand(n, generator=gen)
+            g = g_prev + c * t * d_prev + 1e-3 * torch.randn(n, generator=gen)
             if it in (2, 5):   # negative curvature: y = -s, the pair must be rejected
                 g = g_prev - t * d_prev
             gd, gpd, dd = g.cuda(), g_prev.cuda(), d_prev.cuda()

@@ -202,8 +202,8 @@ class CachePreprocessing:
         for step in range(max_steps + 1):
             mse = torch.mean((target - net(grid)) ** 2)
             if cache_verbose and step:
-                print(f'cache: interpolation step {step}, mse {float(mse)}')
-            if step == max_steps or float(mse) <= tol:
+                print(f'cache: interpolation step {step}, mse {float(mse.detach())}')
+            if step == max_steps or float(mse.detach()) <= tol:
                 break
             opt.zero_grad()
             mse.backward()

@@ -699,17 +699,15 @@ __device__ void zero_rows(unsigned char* buf, int r0, int kp, int es) {
 }  // namespace
 
 struct TcArgs {
-  CUtensorMap dw_map[TDG_MAX_LAYERS];         // per hidden Linear j: dW_j over the gradient segments
   const unsigned char* wpack;                 // packed hidden weights of problem 0
   int64_t wpack_stride;                       // bytes per problem
   int64_t wfwd_off[TDG_MAX_LAYERS];           // byte offsets of W_j (forward) per Linear j
   int64_t wbwd_off[TDG_MAX_LAYERS];           // byte offsets of W_j^T
   int* err;                                   // set when a bounded wait gives up
-  int tma_flush;                              // dW flushes as TMA tensor reductions (dw_map)
 };
 
 template <bool BF16, bool X3, int CM>
-__global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, const __grid_constant__ TcArgs TA) {
+__global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA) {
   constexpr int ES = BF16 ? 2 : 4;
   // TF32 and split TF32 keep every A operand in tensor memory (hi at AHI, lo at ALO), which
   // leaves both shared-memory operand buffers to the B operands; BF16 keeps A in opA
@@ -1369,46 +1367,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, const __g
         cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
       }
       // flush dW_{l-1} (TMEM lane = output neuron, columns = input neurons) into this CTA's zeroed
-      // gradient segment. TMA form: staged in opA (free after the dW MMAs) as the tiles of the
-      // tensor map, four column blocks of [128 rows][32 floats] at 16 KB apart, 128-byte swizzled
-      // (16-byte chunk j of row n at j ^ (n & 7): conflict-free writes); thread 0 then adds each
-      // block into the segment with one cp.reduce.async.bulk.tensor and waits until the TMA
-      // unit has read the stage before anything reuses opA.
-      // (the 128-byte swizzle of the TMA tiles needs opA on a 1024-byte boundary, which the
-      // dynamic shared memory of this kernel starts on; otherwise the atomic form runs)
-      if (TA.tma_flush && (smem_u32(opA) & 1023u) == 0) {
-        const int sw = lrow & 7;
-        auto put = [&](int c, const float (&v)[8]) {
-          float4* row = reinterpret_cast<float4*>(opA + (c >> 5) * 16384 + lrow * 128);
-          const int j = (c & 31) >> 2;
-          row[j ^ sw] = make_float4(v[0], v[1], v[2], v[3]);
-          row[(j + 1) ^ sw] = make_float4(v[4], v[5], v[6], v[7]);
-        };
-        for (int c = 8 * cgrp; c < kp; c += 16 * NCG) {   // two column chunks per wait
-          float v[8], w[8];
-          if (c + 8 * NCG < kp) {
-            tmem_ld8x2(D2 + lane_addr + c, D2 + lane_addr + c + 8 * NCG, v, w);
-            put(c, v);
-            put(c + 8 * NCG, w);
-          } else {
-            tmem_ld8(D2 + lane_addr + c, v);
-            put(c, v);
-          }
-        }
-        fence_async_smem();   // the stage's generic writes before the TMA unit reads it
-        __syncthreads();
-        if (tid == 0) {
-          const int seg = A.tiles[ti].seg;   // re-read: keeps no register live across the tile
-          for (int b = 0; 32 * b < K; ++b)
-            tma_reduce_add_3d(&TA.dw_map[l - 1], opA + b * 16384, 32 * b, 0, seg);
-          bulk_commit();
-          bulk_wait_read0();
-        }
-      } else {
-        // Atomic form: staged in opA as 128 rows of 32 16-byte chunks, chunk j of row n at
-        // j ^ (n & 7) (conflict-free writes and reads), then every warp adds whole rows with
-        // coalesced vector atomics. One thread owns each address in every tile, so the
-        // accumulation order is fixed.
+      // gradient segment: staged in opA (free after the dW MMAs) as 128 rows of 32 16-byte
+      // chunks, chunk j of row n at j ^ (n & 7) (conflict-free writes and reads), then every warp
+      // adds whole rows with coalesced vector atomics. One thread owns each address in every
+      // tile, so the accumulation order is fixed.
+      {
         float4* stage = reinterpret_cast<float4*>(opA);
         const int sw = lrow & 7;
         auto put = [&](int c, const float (&v)[8]) {
@@ -1450,7 +1413,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, const __g
   fence_before();
   __syncthreads();
   cx.drain();
-  if (tid == 0 && TA.tma_flush) bulk_wait0();   // the last dW reductions have completed
   if (warp == 0) tmem_dealloc(*tmem_slot, TMA_A ? 512 : 256);
 }
 
@@ -1509,9 +1471,6 @@ cudaError_t launch_variant(const FusedArgs& a, const TcLaunch& t, int n_ctas, cu
     count_launch();
   }
   TcArgs ta{};
-  ta.tma_flush = t.tma_flush ? 1 : 0;
-  if (t.tma_flush)
-    for (int l = 0; l < TDG_MAX_LAYERS; ++l) ta.dw_map[l] = t.dw_map[l];
   ta.wpack = t.wpack;
   ta.wpack_stride = t.wpack_stride;
   for (int l = 0; l < TDG_MAX_LAYERS; ++l) { ta.wfwd_off[l] = t.fwd_off[l]; ta.wbwd_off[l] = t.bwd_off[l]; }

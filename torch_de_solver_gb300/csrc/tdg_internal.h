@@ -1,7 +1,6 @@
 // Internal tables shared by the host-side plan builder (tdg_plan.cu) and the kernels.
 #pragma once
 #include <cstdint>
-#include <cuda.h>
 #include <cuda_runtime.h>
 #include "../../include/tdg.h"
 
@@ -125,10 +124,6 @@ struct TcLaunch {
   int64_t w_off[TDG_MAX_LAYERS];
   int32_t width[TDG_MAX_LAYERS + 1];
   int* err;
-  // hidden dW flushes as TMA tensor reductions: one map per hidden Linear j over the gradient
-  // segments ([segments][width j+1][width j] floats, 128-byte swizzled [N][32] boxes)
-  const CUtensorMap* dw_map;
-  bool tma_flush;
 };
 size_t fused_tc_smem_bytes();
 

@@ -8,11 +8,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
-#include <mutex>
 #include <string>
 #include <vector>
-
-#include <cudaTypedefs.h>
 
 #include "tdg_internal.h"
 #include "tdg_jetcls.h"
@@ -90,32 +87,12 @@ struct tdg_plan {
   float* d_gy = nullptr;
   double* d_slot_sum = nullptr;
   int64_t wpack_fwd[TDG_MAX_LAYERS] = {0}, wpack_bwd[TDG_MAX_LAYERS] = {0};
-  CUtensorMap dw_map[TDG_MAX_LAYERS];   // TMA maps of the hidden dW over the gradient segments
-  bool tma_flush = false;
   int64_t wpack_stride = 0;
   int64_t workspace_bytes = 0;
   bool arrays_dirty = false;
 };
 
 namespace {
-
-// cuTensorMapEncodeTiled of the driver, looked up once through the runtime (no libcuda link);
-// null when unavailable
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static std::mutex mu;
-  static bool looked = false;
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  std::lock_guard<std::mutex> lock(mu);
-  if (!looked) {
-    looked = true;
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess && q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-  }
-  return fn;
-}
 
 using Key = std::vector<int>;   // sorted axes of a derivative stream
 
@@ -617,24 +594,6 @@ tdg_status tdg_plan_create_scheduled(const tdg_problem_desc* desc, const tdg_sch
       off += np * kp * es;
     }
     p->wpack_stride = off;   // every problem has its own weights
-    // the hidden dW flush as TMA tensor reductions: dW_j ([width j+1][width j] floats, rows of
-    // width j) of every gradient segment as one 3D tensor, 128-byte swizzled [N][32] boxes.
-    // TDG_TMA_FLUSH=0 keeps the vector-atomic flush (an A/B switch; both give the same sums).
-    const char* tf = std::getenv("TDG_TMA_FLUSH");
-    PFN_cuTensorMapEncodeTiled_v12000 enc = (tf && tf[0] == '0') ? nullptr : tensor_map_encoder();
-    p->tma_flush = enc != nullptr && d.form == TDG_FORM_FUSED && L > 2;
-    for (int j = 1; p->tma_flush && j < L - 1; ++j) {
-      const cuuint64_t K = (cuuint64_t)d.mlp.width[j], N = (cuuint64_t)d.mlp.width[j + 1];
-      const cuuint64_t dims[3] = {K, N, (cuuint64_t)p->n_segments};
-      const cuuint64_t strides[2] = {K * sizeof(float), (cuuint64_t)p->part_stride * sizeof(float)};
-      const cuuint32_t box[3] = {32, (cuuint32_t)N, 1};
-      const cuuint32_t elem[3] = {1, 1, 1};
-      const CUresult r = enc(&p->dw_map[j], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, p->d_partial + p->w_off[j],
-                             dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r != CUDA_SUCCESS) p->tma_flush = false;   // the atomic flush stays available
-    }
     if ((st = dev_alloc(p, (void**)&p->d_wpack, (size_t)std::max<int64_t>(off * d.n_problems, 16)))) {
       free_plan(p);
       return st;
@@ -745,8 +704,6 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
     }
     for (int l = 0; l <= p->n_layers; ++l) t.width[l] = p->width[l];
     t.err = p->d_err;
-    t.dw_map = p->dw_map;
-    t.tma_flush = p->tma_flush;
     if (do_grad) {   // the tensor-core kernel accumulates hidden dW with atomic adds
       e = cudaMemsetAsync(p->d_partial, 0, sizeof(float) * p->part_stride * p->n_segments, s);
       if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");

@@ -151,18 +151,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
-// tensor reduce-add of a shared-memory tile into global memory through a tensor map (3D tile
-// coordinates x = innermost), tracked by the issuing thread's bulk async-group
-__device__ __forceinline__ void tma_reduce_add_3d(const void* map, const void* src, int x, int y, int z) {
-  asm volatile("cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
-               :: "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(src)) : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// the shared-memory sources of this thread's committed bulk groups have been read
-__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-// this thread's committed bulk groups have completed
-__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-
 __device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
 }

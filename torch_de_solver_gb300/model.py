@@ -46,7 +46,7 @@ class Model:
         self.batch_size = batch_size
         self._save_dir = os.path.join(tempfile.gettempdir(), 'tedeous_cache/')
         self._graph = None
-        self._check = None   # read by EarlyStopping (tedeous/model.py:46)
+        self._check = None   # read by the reference's early-stopping callback (tedeous/model.py:46)
 
     def compile(self, mode: str, lambda_operator: Union[List[float], float],
                 lambda_bound: Union[List[float], float], normalized_loss_stop: bool = False,
