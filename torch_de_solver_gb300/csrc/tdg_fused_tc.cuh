@@ -1097,6 +1097,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             const int c = lane >> 3, k = 32 * b + 4 * (lane & 7);
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
             if (k < K)
+#pragma unroll 4
               for (int r = c; r < R; r += 4) {
                 const float gy = gybuf[r * MAX_OUT + o];
                 const float4 h = ld4(&P1[r * LDS + k]);
@@ -1122,22 +1123,22 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         }
       }
       __syncthreads();
-      // dL/dH_{L-1} = dL/dY . W: a thread keeps one row (its seeds load once), W rows as vectors
+      // dL/dH_{L-1} = dL/dY . W: consecutive threads take consecutive 4-neuron chunks of one row,
+      // so a warp's seed loads are one broadcast and its W loads and row stores are contiguous
+      // (conflict-free)
       {
-        const int r = tid % RMAX;
-        float g[MAX_OUT];
-#pragma unroll
-        for (int o = 0; o < MAX_OUT; ++o) g[o] = o < d_out && r < R ? gybuf[r * MAX_OUT + o] : 0.f;
-        for (int e = tid; e < RMAX * (kp >> 2); e += NTC) {
-          const int k = (e / RMAX) * 4;
+        const int n4s = kp >> 2;
+        for (int e = tid; e < RMAX * n4s; e += NTC) {
+          const int r = e / n4s, k = (e - r * n4s) * 4;
           float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
           if (r < R && k < K) {
 #pragma unroll
             for (int o = 0; o < MAX_OUT; ++o)
               if (o < d_out) {
+                const float g = gybuf[r * MAX_OUT + o];
                 const float4 w = ld4(&Wl[o * K + k]);
-                v = make_float4(fmaf(g[o], w.x, v.x), fmaf(g[o], w.y, v.y), fmaf(g[o], w.z, v.z),
-                                fmaf(g[o], w.w, v.w));
+                v = make_float4(fmaf(g, w.x, v.x), fmaf(g, w.y, v.y), fmaf(g, w.z, v.z),
+                                fmaf(g, w.w, v.w));
               }
           }
           st4(&P1[r * LDS + k], v);
@@ -1179,21 +1180,24 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           const int n = tid & 127, part = tid >> 7;
           float sb = 0.f;
           float sw[TDG_MAX_DIN] = {0.f, 0.f, 0.f, 0.f};
-          if (n < N)
-            for (int r = RPP * part; r < RPP * part + RPP && r < R; ++r) {
+          const int r_end = RPP * part + RPP < R ? RPP * part + RPP : R;
+          // branch-free and unrolled, so that the rows' loads overlap: a value row adds g to the
+          // bias and g x_a to column a, a first-derivative row along a adds g to column a (adding
+          // zero elsewhere leaves every sum bit for bit as the per-kind branches would)
+          if (n < N) {
+#pragma unroll 4
+            for (int r = RPP * part; r < r_end; ++r) {
               const int ax = row_ax[r];   // -1 value row, else the axis of a first derivative
               const float g = P1[r * LDS + n];
-              if (ax == -1) {
-                sb += g;
+              const float gv = ax == -1 ? g : 0.f;
+              const float4 xv = ld4(&xsbuf[r * TDG_MAX_DIN]);
+              const float xa[TDG_MAX_DIN] = {xv.x, xv.y, xv.z, xv.w};
+              sb += gv;
 #pragma unroll
-                for (int a = 0; a < TDG_MAX_DIN; ++a)
-                  if (a < d_in) sw[a] = fmaf(g, xsbuf[r * TDG_MAX_DIN + a], sw[a]);
-              } else {
-#pragma unroll
-                for (int a = 0; a < TDG_MAX_DIN; ++a)
-                  if (a == ax) sw[a] += g;
-              }
+              for (int a = 0; a < TDG_MAX_DIN; ++a)
+                if (a < d_in) sw[a] = fmaf(gv, xa[a], sw[a]) + (a == ax ? g : 0.f);
             }
+          }
           red[part * 640 + n] = sb;
 #pragma unroll
           for (int a = 0; a < TDG_MAX_DIN; ++a) red[part * 640 + 128 * (1 + a) + n] = sw[a];
