@@ -546,10 +546,12 @@ __device__ void rows_to_opT(const float* __restrict__ P, unsigned char* __restri
     float v[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) v[i] = r + i < R ? P[(r + i) * LDS + n] : 0.f;
-    if (X3) {   // hi rounded once, stored as it is; lo = x - hi, rounded by put4
+    if (X3) {   // hi rounded to TF32; lo = x - hi stored as it is (the MMA takes its TF32 bits,
+                // as for every other low part)
       const float4 h = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
       *reinterpret_cast<float4*>(dst + ofs(n, rl, nr, 4)) = h;
-      put4<false>(dst + lo_off, n, rl, nr, make_float4(v[0] - h.x, v[1] - h.y, v[2] - h.z, v[3] - h.w));
+      *reinterpret_cast<float4*>(dst + lo_off + ofs(n, rl, nr, 4)) =
+          make_float4(v[0] - h.x, v[1] - h.y, v[2] - h.z, v[3] - h.w);
     } else {
       put4<BF16>(dst, n, rl, nr, make_float4(v[0], v[1], v[2], v[3]));
     }
@@ -1153,6 +1155,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         prefetch_l2(scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * p16(A.width[l - 1]) * 4));
       // Z_l (scratch slot l-1, interleaved FP32) -> opB, issued ahead
       cx.ensure(opB, scr + (int64_t)(l - 1) * scr_slot, (uint32_t)(128 * np * 4));
+
       // jet adjoint: P1 (dL/dH_l) -> P1 (dL/dZ_l) in place, streams of a site in increasing order;
       // also the K-major operand copy of dL/dZ_l in opA for the dX GEMM
       {
@@ -1229,6 +1232,13 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
         }
         cx.publish();
+      }
+      // Z_l (scratch slot l-1) reached opB for the last time at the top of this layer: warps
+      // other than the MMA issuer's drop its lines from L2 (no write-back to DRAM; the next tile's
+      // forward rewrites them) while the dX GEMM's weights land and its MMAs run
+      if (warp > 0) {
+        const char* zg = reinterpret_cast<const char*>(scr + (int64_t)(l - 1) * scr_slot);
+        for (int off = (tid - 32) * 128; off < 128 * np * 4; off += (NTC - 32) * 128) discard_l2(zg + off);
       }
       // dX: D1[rows x kp] = dL/dZ_l[rows x np] . (W_{l-1}^T packed [kp x np])^T
       if constexpr (TMA_A) {

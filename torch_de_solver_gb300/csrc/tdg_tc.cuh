@@ -151,6 +151,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
+// invalidate one 128-byte line of global memory in L2 without writing it back (its contents
+// become unspecified): for scratch that nothing reads again
+__device__ __forceinline__ void discard_l2(const void* line) {
+  asm volatile("discard.global.L2 [%0], 128;" :: "l"(line) : "memory");
+}
+
 __device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
 }
