@@ -541,8 +541,9 @@ __device__ void jet_rows_from_op(const unsigned char* __restrict__ zs, float* __
 template <bool BF16, bool X3>
 __device__ void rows_to_opT(const float* __restrict__ P, unsigned char* __restrict__ dst, int kp, int r_lo,
                             int nr, int R, uint32_t lo_off) {
+  const bool k128 = kp == 128;   // shifts instead of a runtime division for the common width
   for (int e = threadIdx.x; e < kp * (nr >> 2); e += NTC) {
-    const int n = e % kp, rl = 4 * (e / kp), r = r_lo + rl;
+    const int n = k128 ? e & 127 : e % kp, rl = 4 * (k128 ? e >> 7 : e / kp), r = r_lo + rl;
     float v[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) v[i] = r + i < R ? P[(r + i) * LDS + n] : 0.f;
@@ -554,6 +555,30 @@ __device__ void rows_to_opT(const float* __restrict__ P, unsigned char* __restri
           make_float4(v[0] - h.x, v[1] - h.y, v[2] - h.z, v[3] - h.w);
     } else {
       put4<BF16>(dst, n, rl, nr, make_float4(v[0], v[1], v[2], v[3]));
+    }
+  }
+}
+
+// split TF32, 128 neurons: rows [0, 64) of P transposed into dst0 and rows [64, 128) into dst1 (each
+// [hi | lo], lo at lo_off), as rows_to_opT with compile-time index arithmetic: thread t keeps
+// neuron t % 128 and takes the 4-row groups (t / 128) + 4 i of each half
+__device__ __forceinline__ void rows_to_opT_x3_128(const float* __restrict__ P, unsigned char* __restrict__ dst0,
+                                                   unsigned char* __restrict__ dst1, int R, uint32_t lo_off) {
+  static_assert(NTC % 128 == 0, "a thread keeps its neuron");
+  const int n = threadIdx.x & 127;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    unsigned char* dst = h ? dst1 : dst0;
+#pragma unroll
+    for (int i = 0; i < 64 / 4 / (NTC / 128); ++i) {
+      const int rl = 4 * ((int)(threadIdx.x >> 7) + (NTC / 128) * i), r = 64 * h + rl;
+      float v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = r + j < R ? P[(r + j) * LDS + n] : 0.f;
+      const float4 hv = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+      const uint32_t o = ofs(n, rl, 64, 4);
+      *reinterpret_cast<float4*>(dst + o) = hv;
+      *reinterpret_cast<float4*>(dst + lo_off + o) = make_float4(v[0] - hv.x, v[1] - hv.y, v[2] - hv.z, v[3] - hv.w);
     }
   }
 }
@@ -628,9 +653,9 @@ __device__ void rows_to_tmem(const float* __restrict__ P, uint32_t a_hi, uint32_
 // the packed B from global memory: split TF32 streams K-half 0 ([hi | lo]) through slot A into
 // bufA and K-half 1 through slot B into bufB, and issues K-half 0's MMAs while K-half 1 lands;
 // TF32 takes all of B through slot A. Copies issued ahead are waited for, not reissued.
-template <bool X3>
+template <bool X3, typename F>
 __device__ void gemm_tmem_a(TcCtx& cx, uint32_t d, uint32_t a_hi, uint32_t a_lo, unsigned char* bufA,
-                            unsigned char* bufB, const unsigned char* b_src, int n, int k) {
+                            unsigned char* bufB, const unsigned char* b_src, int n, int k, F&& during) {
   const uint32_t idesc = instr_desc<false>(128, n);
   if (X3) {
     const int kh = k / 2;
@@ -670,18 +695,22 @@ __device__ void gemm_tmem_a(TcCtx& cx, uint32_t d, uint32_t a_hi, uint32_t a_lo,
       commit(cx.bar_mma);
     }
   }
+  during();   // every thread: work that touches neither the operands nor the accumulator
   cx.wait_mma();
 }
 
 // dL/dH rows from the dX accumulator (tensor memory) into plain FP32 rows, zero past K and R
 __device__ __forceinline__ void d1_to_rows(uint32_t d1, float* __restrict__ P, int kp, int K, int R,
                                            uint32_t lane_addr, int lrow, int cgrp) {
+  const bool plain = K == kp && lrow < R;   // nothing to mask
   for (int c = 8 * cgrp; c < kp; c += 8 * NCG) {
     float v[8];
     tmem_ld8(d1 + lane_addr + c, v);
+    if (!plain) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-      if (lrow >= R || c + i >= K) v[i] = 0.f;
+      for (int i = 0; i < 8; ++i)
+        if (lrow >= R || c + i >= K) v[i] = 0.f;
+    }
     st4(&P[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
     st4(&P[lrow * LDS + c + 4], make_float4(v[4], v[5], v[6], v[7]));
   }
@@ -691,8 +720,9 @@ __device__ __forceinline__ void d1_to_rows(uint32_t d1, float* __restrict__ P, i
 template <bool BF16>
 __device__ void zero_rows(unsigned char* buf, int r0, int kp, int es) {
   const int n4s = kp >> 2;
+  const bool k128 = kp == 128;
   for (int e = threadIdx.x; e < (128 - r0) * n4s; e += NTC) {
-    const int r = r0 + e / n4s, n = (e % n4s) * 4;
+    const int r = r0 + (k128 ? e >> 5 : e / n4s), n = (k128 ? e & 31 : e % n4s) * 4;
     if (es == 4) *reinterpret_cast<float4*>(buf + ofs(r, n, kp, 4)) = make_float4(0, 0, 0, 0);
     else *reinterpret_cast<uint2*>(buf + ofs(r, n, kp, 2)) = make_uint2(0, 0);
   }
@@ -821,18 +851,11 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
     }
     const DevGroup& G = *Gs;
     const int T = G.T, S = G.S, R = T * S;
+    // e / T for 0 <= e < 2^16 as one multiply-high: tmag = ceil(2^32 / T), exact since e T < 2^32
+    const uint32_t tmag = 0xFFFFFFFFu / (uint32_t)T + 1u;
+    auto divT = [&](int e) { return (int)__umulhi((uint32_t)e, tmag); };
     const int nvalid = tile.nvalid, row0 = tile.row0;
 
-    for (int e = tid; e < RMAX * d_in; e += NTC) {
-      const int r = e / d_in, a = e - r * d_in;
-      float x = 0.f;
-      if (r < R) {
-        const int s = r / T, p = r - s * T, q = G.st_site[s];
-        if (p < nvalid) x = A.arrays[G.site_points[q]][(int64_t)(row0 + p) * d_in + a] + G.site_off[q][a];
-      }
-      xsbuf[r * TDG_MAX_DIN + a] = x;
-    }
-    __syncthreads();
 
     // ---- input layer -> Z_1 (plain in P1, interleaved FP32 in scratch slot 0)
     {
@@ -848,9 +871,23 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       unsigned char* s0 = reinterpret_cast<unsigned char*>(scr);
       auto layer = [&](auto din) {
         constexpr int D = decltype(din)::value;
+        // the coordinates of this thread's row, loaded by the thread itself (no barrier); the
+        // threads of the first 128 also keep them in xsbuf for the input-layer gradients
         float x[D];
 #pragma unroll
-        for (int a = 0; a < D; ++a) x[a] = xsbuf[r * TDG_MAX_DIN + a];
+        for (int a = 0; a < D; ++a) x[a] = 0.f;
+        if (r < R) {
+          const int s = r / T, p = r - s * T, q = G.st_site[s];
+          if (p < nvalid) {
+            const float* src = A.arrays[G.site_points[q]] + (int64_t)(row0 + p) * D;
+#pragma unroll
+            for (int a = 0; a < D; ++a) x[a] = src[a] + G.site_off[q][a];
+          }
+        }
+        if (tid < RMAX) {
+#pragma unroll
+          for (int a = 0; a < D; ++a) xsbuf[r * TDG_MAX_DIN + a] = x[a];
+        }
         for (int e = tid; e < RMAX * (np >> 2); e += NTC) {
           const int n = (e / RMAX) * 4;
           float z[4] = {0.f, 0.f, 0.f, 0.f};
@@ -913,7 +950,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const int K = A.width[j], N = A.width[j + 1];
       const int kp = p16(K), np = p16(N);
       if constexpr (TMA_A) {
-        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, wpk + TA.wfwd_off[j], np, kp);
+        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, wpk + TA.wfwd_off[j], np, kp, [] {});
       } else if (X3) {
         gemm3x(cx, D1, opA, ALO, opB, wpk + TA.wfwd_off[j], np, kp);
       } else {
@@ -928,16 +965,25 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const float* bj = pbuf + PB_HB + (j - 1) * TDG_MAX_WIDTH;
         const bool val = row_v[lrow] != 0;
         unsigned char* sj = reinterpret_cast<unsigned char*>(scr + (int64_t)j * scr_slot);
+        // a full-width layer and a filled row need no masks: v + 1 * b on value rows, v + 0 * b
+        // on the others (the same sums as the masked form)
+        const bool plain = N == np && lrow < R;
+        const float vb = val ? 1.f : 0.f;
         for (int c = 8 * cgrp; c < np; c += 8 * NCG) {
           float v[8];
           tmem_ld8(D1 + lane_addr + c, v);
           const float4 b0v = ld4(&bj[c]), b1v = ld4(&bj[c + 4]);
           const float bb[8] = {b0v.x, b0v.y, b0v.z, b0v.w, b1v.x, b1v.y, b1v.z, b1v.w};
+          if (plain) {
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int n = c + i;
-            v[i] = n < N ? v[i] + (val ? bb[i] : 0.f) : 0.f;
-            if (lrow >= R) v[i] = 0.f;
+            for (int i = 0; i < 8; ++i) v[i] = fmaf(vb, bb[i], v[i]);
+          } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              const int n = c + i;
+              v[i] = n < N ? v[i] + (val ? bb[i] : 0.f) : 0.f;
+              if (lrow >= R) v[i] = 0.f;
+            }
           }
           st4(&P1[lrow * LDS + c], make_float4(v[0], v[1], v[2], v[3]));
           st4(&P1[lrow * LDS + c + 4], make_float4(v[4], v[5], v[6], v[7]));
@@ -1001,7 +1047,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       double* e2 = reinterpret_cast<double*>(seedv + MAX_OUT * RMAX);   // [MAX_OUT][T]
       const int nt = G.n_terms;
       for (int e = tid; e < T * nt; e += NTC) {
-        const int p = e % T, t = e / T;
+        const int t = divT(e), p = e - t * T;
         const DevTerm& tm = G.terms[t];
         const bool valid = p < nvalid;
         const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
@@ -1019,7 +1065,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
       __syncthreads();
       for (int e = tid; e < T * n_out; e += NTC) {
-        const int p = e % T, o = e / T;
+        const int o = divT(e), p = e - o * T;
         const bool valid = p < nvalid;
         float out = 0.f;
         for (int t = 0; t < nt; ++t)
@@ -1041,7 +1087,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
       if (A.do_grad) {
         for (int e = tid; e < T * nt; e += NTC) {
-          const int p = e % T, t = e / T;
+          const int t = divT(e), p = e - t * T;
           const DevTerm& tm = G.terms[t];
           const bool valid = p < nvalid;
           const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
@@ -1130,8 +1176,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       // (conflict-free)
       {
         const int n4s = kp >> 2;
+        const bool k128 = kp == 128;   // compile-time index arithmetic for the common width
         for (int e = tid; e < RMAX * n4s; e += NTC) {
-          const int r = e / n4s, k = (e - r * n4s) * 4;
+          const int r = k128 ? e >> 5 : e / n4s, k = k128 ? (e & 31) * 4 : (e - r * n4s) * 4;
           float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
           if (r < R && k < K) {
 #pragma unroll
@@ -1209,7 +1256,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         float* dW0 = grad + A.w_off[0];
         float* db0 = grad + A.b_off[0];
         for (int e = tid; e < N * (1 + d_in); e += NTC) {
-          const int n = e % N, c = e / N;   // c = 0: bias, c = 1 + a: weight column a
+          const int n = N == 128 ? e & 127 : e % N, c = N == 128 ? e >> 7 : e / N;   // c = 0: bias, c = 1 + a: weight column a
           float v = red[128 * c + n];
 #pragma unroll
           for (int q = 1; q < NPART; ++q) v += red[640 * q + 128 * c + n];
@@ -1242,7 +1289,22 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       }
       // dX: D1[rows x kp] = dL/dZ_l[rows x np] . (W_{l-1}^T packed [kp x np])^T
       if constexpr (TMA_A) {
-        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, wpk + TA.wbwd_off[l - 1], kp, np);
+        // while the MMAs run: the bias gradient partials of Linear l-1 (sums of dL/dZ_l over the
+        // value rows of row blocks 8 (q + 4 i), q = this thread's part) from P1, into ybuf
+        gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, wpk + TA.wbwd_off[l - 1], kp, np, [&] {
+          const int n = tid & 127, q = tid >> 7;
+          float sb = 0.f;
+          if (n < N) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int rr = 0; rr < 8; ++rr) {
+                const int r = 8 * (q + 4 * i) + rr;
+                if (row_v[r]) sb += P1[r * LDS + n];
+              }
+          }
+          ybuf[q * 128 + n] = sb;
+        });
       } else if (X3) {
         gemm3x(cx, D1, opA, ALO, opB, wpk + TA.wbwd_off[l - 1], kp, np);
       } else {
@@ -1266,7 +1328,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
               v[i] = (n < N && r + i < R) ? P1[(r + i) * LDS + n] : 0.f;
-              if (row_v[r + i]) sb += v[i];
               h[i] = to_tf32(v[i]);
             }
             tmem_st8(AHI + lane_addr + r, h);
@@ -1282,7 +1343,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             v[i] = (n < N && r + i < R) ? P1[(r + i) * LDS + n] : 0.f;
-            if (row_v[r + i]) sb += v[i];
+            if (!TMA_A && row_v[r + i]) sb += v[i];
           }
           if constexpr (TMA_A) {   // lane = neuron n, columns = rows r..r+3 (the same r for the warp)
             tmem_st4(AHI + lane_addr + r, to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
@@ -1294,7 +1355,7 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           }
         }
         if (TMA_A || X3) tmem_st_wait();
-        red[(tid >> 7) * 128 + n] = sb;
+        if (!TMA_A) red[(tid >> 7) * 128 + n] = sb;   // TMA_A: written while the dX MMAs ran
         __syncthreads();
         float* db = grad + A.b_off[l - 1];
         for (int m = tid; m < N; m += NTC) {
@@ -1304,7 +1365,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           red_add1(&db[m], v);
         }
       }
-      cx.publish();
+      // no barrier here: the H rows below overwrite P1, which every thread finished reading
+      // before the barrier above, and the bias partials are not written again in this layer
+      if constexpr (!TMA_A) cx.publish();
       // H_{l-1}: the tanh jets of Z_{l-1} (opB) per (point, 4 neurons), every stream of a site
       // at once, as FP32 rows in P1 (dL/dZ_l there is consumed)
       cx.wait_tma();
@@ -1316,8 +1379,12 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         const uint32_t idesc = instr_desc<false>(128, kp);
         if (X3) {
           const uint32_t lo_off = (uint32_t)kp * 64 * 4;
-          rows_to_opT<false, true>(P1, opA, kp, 0, 64, R, lo_off);
-          rows_to_opT<false, true>(P1, opB, kp, 64, 64, R, lo_off);
+          if (kp == 128) {
+            rows_to_opT_x3_128(P1, opA, opB, R, lo_off);
+          } else {
+            rows_to_opT<false, true>(P1, opA, kp, 0, 64, R, lo_off);
+            rows_to_opT<false, true>(P1, opB, kp, 64, 64, R, lo_off);
+          }
           cx.publish();
           if (tid == 0) {
             for (int hh = 0; hh < 2; ++hh) {
