@@ -1021,15 +1021,22 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const float* bl = pbuf + PB_BL;
       for (int e = tid; e < RMAX * d_out; e += NTC) {
         const int r = e % RMAX, o = e / RMAX;
-        float z = 0.f;
+        // four independent chains (16-byte chunks c, c + 4, ...), summed pairwise at the end
+        float zc[4] = {0.f, 0.f, 0.f, 0.f};
         const float* w = &Wl[(int64_t)o * K];
-        for (int k = 0; k < K; k += 4) {
-          const float4 hv = ld4(&P1[r * LDS + k]);
-          z = fmaf(hv.x, w[k], z);
-          z = fmaf(hv.y, w[k + 1], z);
-          z = fmaf(hv.z, w[k + 2], z);
-          z = fmaf(hv.w, w[k + 3], z);
+        for (int k = 0; k < K; k += 16) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (k + 4 * c < K) {
+              const float4 hv = ld4(&P1[r * LDS + k + 4 * c]), wv = ld4(&w[k + 4 * c]);
+              zc[c] = fmaf(hv.x, wv.x, zc[c]);
+              zc[c] = fmaf(hv.y, wv.y, zc[c]);
+              zc[c] = fmaf(hv.z, wv.z, zc[c]);
+              zc[c] = fmaf(hv.w, wv.w, zc[c]);
+            }
+          }
         }
+        float z = (zc[0] + zc[1]) + (zc[2] + zc[3]);
         if (row_v[r]) z += bl[o];
         ybuf[r * MAX_OUT + o] = z;
         gybuf[r * MAX_OUT + o] = 0.f;
@@ -1080,10 +1087,13 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = out;
       }
       __syncthreads();
-      if (tid < n_out) {   // fixed-order FP64 sum over the tile's points
+      if (warp < n_out) {   // FP64 sum over the tile's points, one warp per output, fixed order:
+                            // lane-strided partial sums, then a butterfly
         double sum = 0.0;
-        for (int p = 0; p < T; ++p) sum += e2[tid * RMAX + p];
-        cur_slot[tid] += sum;
+        for (int p = lane; p < T; p += 32) sum += e2[warp * RMAX + p];
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, m);
+        if (lane == 0) cur_slot[warp] += sum;
       }
       if (A.do_grad) {
         for (int e = tid; e < T * nt; e += NTC) {
@@ -1325,11 +1335,15 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             if (e >= 128 * 16) break;
             const int r = (e >> 7) * 8;
             float v[8], h[8];
+            if (n < N && r + 8 <= R) {   // a full block of rows: no masks
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              v[i] = (n < N && r + i < R) ? P1[(r + i) * LDS + n] : 0.f;
-              h[i] = to_tf32(v[i]);
+              for (int i = 0; i < 8; ++i) v[i] = P1[(r + i) * LDS + n];
+            } else {
+#pragma unroll
+              for (int i = 0; i < 8; ++i) v[i] = (n < N && r + i < R) ? P1[(r + i) * LDS + n] : 0.f;
             }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) h[i] = to_tf32(v[i]);
             tmem_st8(AHI + lane_addr + r, h);
             if (X3) {
 #pragma unroll
