@@ -52,7 +52,8 @@ extern "C" {
 #define TDG_MAX_LAYERS 12      /* Linear layers of the MLP */
 #define TDG_MAX_DIN 4          /* input coordinates per point */
 #define TDG_MAX_DOUT 8         /* MLP outputs (dependent variables) */
-#define TDG_MAX_WIDTH 128      /* hidden width */
+#define TDG_MAX_WIDTH 128      /* hidden width of the fused forms (a multiple of 4) */
+#define TDG_MAX_WIDTH_PLAIN 4096 /* hidden width of the plain form (any width) */
 #define TDG_MAX_ORDER 3        /* derivative order of one stream */
 #define TDG_MAX_STREAMS 16     /* (site, stream) pairs per row */
 #define TDG_MAX_SITES 16       /* evaluation sites per row */

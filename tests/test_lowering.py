@@ -256,3 +256,24 @@ def test_shard_ir_splits_residual_rows():
     assert ir.groups[ir.residual_group].n_rows == res.n_rows == 121   # the original is untouched
     with pytest.raises(ValueError):
         shard_rows(10, 3, 3)
+
+
+def test_form_choice_by_hidden_width():
+    """form=None: the fused form for hidden widths that are multiples of 4 up to 128, otherwise the
+    plain form (FP32, any width) with a warning; a tensor-core precision with such a network raises,
+    and an explicit form is kept as given (the plan then names its own limit)."""
+    import warnings
+    from torch_de_solver_gb300.solution import default_form, fused_width_ok
+    assert fused_width_ok([2, 128, 128, 3]) and fused_width_ok([2, 4, 1])
+    assert not fused_width_ok([2, 50, 50, 1]) and not fused_width_ok([2, 256, 1])
+    with warnings.catch_warnings():
+        warnings.simplefilter('error')
+        assert default_form([2, 100, 100, 1], None, None) == 'fused'
+        assert default_form([2, 100, 100, 1], 'bf16', None) == 'fused'
+        assert default_form([2, 150, 1], None, 'fused') == 'fused'
+    for precision in (None, 'fp32'):
+        with pytest.warns(UserWarning, match='plain form'):
+            assert default_form([2, 150, 150, 1], precision, None) == 'plain'
+    for precision in ('3xtf32', 'tf32', 'bf16'):
+        with pytest.raises(NotImplementedError, match='hidden widths'):
+            default_form([2, 50, 1], precision, None)

@@ -14,7 +14,8 @@ LIB_PATH = os.path.join(_HERE, 'libtdg.so')
 MAX_LAYERS = 12
 MAX_DIN = 4
 MAX_DOUT = 8
-MAX_WIDTH = 128
+MAX_WIDTH = 128          # the fused forms: hidden widths that are multiples of 4, up to this
+MAX_WIDTH_PLAIN = 4096   # the plain form: any hidden width up to this
 MAX_ORDER = 3
 MAX_STREAMS = 16
 MAX_SITES = 16

@@ -404,8 +404,17 @@ tdg_status tdg_plan_create_scheduled(const tdg_problem_desc* desc, const tdg_sch
   if (d_in < 1 || d_in > TDG_MAX_DIN) return fail(TDG_ERR_UNSUPPORTED, "input width %d (1..%d)", d_in, TDG_MAX_DIN);
   if (d_out < 1 || d_out > TDG_MAX_DOUT) return fail(TDG_ERR_UNSUPPORTED, "output width %d (1..%d)", d_out, TDG_MAX_DOUT);
   for (int l = 1; l < L; ++l) {
+    // the fused kernels keep a layer's rows and operands on chip and move them in 16-byte
+    // vectors; the plain form's per-layer kernels take any width
     const int w = d.mlp.width[l];
-    if (w < 4 || w > TDG_MAX_WIDTH || w % 4) return fail(TDG_ERR_UNSUPPORTED, "hidden width %d (multiple of 4, <= %d)", w, TDG_MAX_WIDTH);
+    if (d.form == TDG_FORM_PLAIN) {
+      if (w < 1 || w > TDG_MAX_WIDTH_PLAIN)
+        return fail(TDG_ERR_UNSUPPORTED, "hidden width %d (the plain form takes 1..%d)", w, TDG_MAX_WIDTH_PLAIN);
+    } else if (w < 4 || w > TDG_MAX_WIDTH || w % 4) {
+      return fail(TDG_ERR_UNSUPPORTED,
+                  "hidden width %d (the fused form takes a multiple of 4, <= %d; the plain form any width up to %d)",
+                  w, TDG_MAX_WIDTH, TDG_MAX_WIDTH_PLAIN);
+    }
   }
   if (d.precision < TDG_PREC_FP32 || d.precision > TDG_PREC_BF16)
     return fail(TDG_ERR_UNSUPPORTED, "precision %d not built", d.precision);

@@ -52,13 +52,15 @@ class Model:
                 lambda_bound: Union[List[float], float], normalized_loss_stop: bool = False,
                 h: float = 0.001, inner_order: str = '1', boundary_order: str = '2',
                 derivative_points: int = 2, weak_form: List[callable] = None, tol: float = 0,
-                removed_domains: list = None, precision: str = None, form: str = 'fused',
+                removed_domains: list = None, precision: str = None, form: str = None,
                 autotune: bool = False):
         """Arguments as in tedeous/model.py:56-113, plus precision and form ('fused' or 'plain').
         precision: '3xtf32' (split-TF32 tensor cores at FP32 tolerance; the default of the fused
         form), 'fp32' (CUDA cores, bitwise reproducible gradient; the plain form's only one),
-        'tf32' or 'bf16'. autotune=True picks the fused kernel's tile schedule by timing
-        candidates on the device (torch_de_solver_gb300.autotune)."""
+        'tf32' or 'bf16'. form=None is the fused form when the network's hidden widths are
+        multiples of 4 up to 128, else the plain form (any width; see solution.default_form).
+        autotune=True picks the fused kernel's tile schedule by timing candidates on the device
+        (torch_de_solver_gb300.autotune)."""
         if weak_form:
             raise NotImplementedError('weak-form losses are not implemented on the device path')
         self.mode = mode

@@ -12,11 +12,35 @@ per-parameter views.
 """
 
 import ctypes
+import warnings
 
 import torch
 
 from . import _lib
 from .prepare import CoeffParam, lower, shard_ir
+
+
+def fused_width_ok(widths):
+    """Whether the fused kernels take these hidden widths (multiples of 4, at most MAX_WIDTH)."""
+    return all(w % 4 == 0 and 4 <= w <= _lib.MAX_WIDTH for w in widths[1:-1])
+
+
+def default_form(widths, precision, form):
+    """form=None selects the fused form, unless a hidden width is one the fused kernels do not
+    take (not a multiple of 4, or above 128, e.g. the 50-, 150- and 256-wide networks of the
+    reference's examples): then the plain form, which takes any width and computes in FP32,
+    with a warning. A tensor-core precision asked for with such a network raises."""
+    if form is not None:
+        return form
+    if fused_width_ok(widths):
+        return 'fused'
+    if precision not in (None, 'fp32'):
+        raise NotImplementedError(
+            f'hidden widths {widths[1:-1]}: precision {precision!r} runs in the fused form, which '
+            f'takes multiples of 4 up to {_lib.MAX_WIDTH}; the plain form (FP32) takes any width')
+    warnings.warn(f'hidden widths {widths[1:-1]} are outside the fused kernels (multiples of 4 up '
+                  f'to {_lib.MAX_WIDTH}): the step runs in the plain form (per-layer FP32 kernels)')
+    return 'plain'
 
 
 def default_precision(precision, form):
@@ -320,7 +344,7 @@ class Solution:
     and GPU) and builds the plans with the fastest."""
 
     def __init__(self, grid, operator, bconds, model, mode, lambda_operator, lambda_bound,
-                 h=0.001, inner_order='1', boundary_order='2', precision=None, form='fused',
+                 h=0.001, inner_order='1', boundary_order='2', precision=None, form=None,
                  device=None, tol=0, batch_size=None, shard=None, autotune=False):
         if not torch.cuda.is_available():
             raise RuntimeError('torch_de_solver_gb300 runs on a CUDA device; none is available')
@@ -329,8 +353,9 @@ class Solution:
         self.mode = mode
         self.grid = grid
         self.lambda_operator, self.lambda_bound = lambda_operator, lambda_bound
-        self.precision, self.form = default_precision(precision, form), form
         widths = mlp_widths(model)
+        form = default_form(widths, precision, form)
+        self.precision, self.form = default_precision(precision, form), form
         if batch_size is not None and mode == 'NN' and tol:
             raise NotImplementedError("the causal loss with mini-batches in 'NN' mode (the "
                                       "reference's time-slice count fails there)")
