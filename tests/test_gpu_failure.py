@@ -31,8 +31,8 @@ def test_invalid_descriptions_fail_before_launch():
     from torch_de_solver_gb300 import _lib
     d, b, e, net, kw = cases.burgers_ag(T, n=8, widths=(2, 30, 30, 1))   # width not a multiple of 4
     m = T.Model(net, d, e, b)
-    with pytest.raises(NotImplementedError):
-        m.compile('autograd', lambda_operator=1, lambda_bound=1)
+    with pytest.raises(NotImplementedError):   # the fused form asked for: the plan refuses it
+        m.compile('autograd', lambda_operator=1, lambda_bound=1, form='fused')
     d, b, e, net, kw = cases.burgers_ag(T, n=8)
     m = T.Model(net, d, e, b)
     with pytest.raises(NotImplementedError):
