@@ -70,12 +70,12 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
       }
     }
   }
-  const int T = G.T;
+  const FastDiv fdT(G.T);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int r = ty + 16 * i;
     if (r >= R) continue;
-    const bool val = G.st_order[r / T] == 0;
+    const bool val = G.st_order[fdT.div(r)] == 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int n = tx + 16 * j;
@@ -175,12 +175,13 @@ __device__ void gemm_dw(const float* __restrict__ Gz, const float* __restrict__ 
       *dst = v;
     }
   }
-  // bias gradient: one thread per neuron
+  // bias gradient: one thread per neuron, the value streams' rows in ascending order
   const int T = G.T;
   for (int n = threadIdx.x; n < N; n += NT) {
     float s = 0.f;
-    for (int r = 0; r < R; ++r)
-      if (G.st_order[r / T] == 0) s += Gz[r * LDS + n];
+    for (int st = 0; st * T < R; ++st)
+      if (G.st_order[st] == 0)
+        for (int r = st * T; r < st * T + T && r < R; ++r) s += Gz[r * LDS + n];
     db[n] = first ? s : db[n] + s;
   }
 }
@@ -251,8 +252,9 @@ __device__ __noinline__ void coeff_grad_warps(const DevGroup& G, const DevTerm* 
 
 __device__ void jet_forward(float* __restrict__ buf, const DevGroup& G, int N) {
   const int T = G.T;
+  const FastDiv fdN(N);
   for (int e = threadIdx.x; e < T * N; e += NT) {
-    const int p = e / N, n = e - p * N;
+    const int p = fdN.div(e), n = e - p * N;
     for (int q = 0; q < G.n_sites; ++q) {
       const int ns = G.site_nstreams[q];
       const int base = G.site_streams[q][0];
@@ -282,8 +284,9 @@ __device__ void jet_forward(float* __restrict__ buf, const DevGroup& G, int N) {
 __device__ void jet_backward(const float* __restrict__ zbuf, float* __restrict__ gbuf,
                              const DevGroup& G, int N) {
   const int T = G.T;
+  const FastDiv fdN(N);
   for (int e = threadIdx.x; e < T * N; e += NT) {
-    const int p = e / N, n = e - p * N;
+    const int p = fdN.div(e), n = e - p * N;
     for (int q = 0; q < G.n_sites; ++q) {
       const int ns = G.site_nstreams[q];
       const int base = G.site_streams[q][0];
@@ -319,14 +322,16 @@ __device__ void jet_backward(const float* __restrict__ zbuf, float* __restrict__
 __device__ void load_weights(float* __restrict__ wbuf, const float* __restrict__ W, int N, int K) {
   if ((reinterpret_cast<uintptr_t>(W) & 15) == 0) {
     const int K4 = K >> 2;
+    const FastDiv fdK4(K4);
     for (int e = threadIdx.x; e < N * K4; e += NT) {
-      const int n = e / K4, k = (e - n * K4) * 4;
+      const int n = fdK4.div(e), k = (e - n * K4) * 4;
       *reinterpret_cast<float4*>(&wbuf[n * LDS + k]) =
           __ldg(reinterpret_cast<const float4*>(&W[(int64_t)n * K + k]));
     }
   } else {
+    const FastDiv fdK(K);
     for (int e = threadIdx.x; e < N * K; e += NT) {
-      const int n = e / K, k = e - n * K;
+      const int n = fdK.div(e), k = e - n * K;
       wbuf[n * LDS + k] = __ldg(&W[(int64_t)n * K + k]);
     }
   }
@@ -334,8 +339,9 @@ __device__ void load_weights(float* __restrict__ wbuf, const float* __restrict__
 
 __device__ void copy_rows(float* __restrict__ dst, const float* __restrict__ src, int R, int K) {
   const int K4 = K >> 2;
+  const FastDiv fdK4(K4);
   for (int e = threadIdx.x; e < R * K4; e += NT) {
-    const int r = e / K4, k = (e - r * K4) * 4;
+    const int r = fdK4.div(e), k = (e - r * K4) * 4;
     *reinterpret_cast<float4*>(&dst[r * LDS + k]) = *reinterpret_cast<const float4*>(&src[r * LDS + k]);
   }
 }
@@ -383,13 +389,14 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     }
     const DevGroup& G = *Gs;
     const int T = G.T, S = G.S, R = T * S;
+    const FastDiv fdT(T);
     const int nvalid = tile.nvalid, row0 = tile.row0;
     const float* prm = A.params + (int64_t)G.problem * A.n_params;
 
     // ---- coordinates of every row (site point + FP32 offset), zero for padding points
     for (int e = tid; e < R * d_in; e += NT) {
       const int r = e / d_in, a = e - r * d_in;
-      const int s = r / T, p = r - s * T;
+      const int s = fdT.div(r), p = r - s * T;
       const int q = G.st_site[s];
       float x = 0.f;
       if (p < nvalid) x = A.arrays[G.site_points[q]][(int64_t)(row0 + p) * d_in + a] + G.site_off[q][a];
@@ -402,9 +409,10 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       const int N = A.width[1];
       const float* W0 = prm + A.w_off[0];
       const float* b0 = prm + A.b_off[0];
+      const FastDiv fdN(N);
       for (int e = tid; e < R * N; e += NT) {
-        const int r = e / N, n = e - r * N;
-        const int s = r / T;
+        const int r = fdN.div(e), n = e - r * N;
+        const int s = fdT.div(r);
         const int o = G.st_order[s];
         float z;
         if (o == 0) {
@@ -456,7 +464,7 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
           z = fmaf(hv.z, __ldg(&w[k + 2]), z);
           z = fmaf(hv.w, __ldg(&w[k + 3]), z);
         }
-        if (G.st_order[r / T] == 0) z += __ldg(&bl[o]);
+        if (G.st_order[fdT.div(r)] == 0) z += __ldg(&bl[o]);
         ybuf[r * MAX_OUT + o] = z;
         gybuf[r * MAX_OUT + o] = 0.f;
       }
@@ -567,20 +575,22 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       const float* Wl = prm + A.w_off[L - 1];
       float* dW = grad + A.w_off[L - 1];
       float* db = grad + A.b_off[L - 1];
+      const FastDiv fdK(K);
       for (int e = tid; e < d_out * K; e += NT) {
-        const int o = e / K, k = e - o * K;
+        const int o = fdK.div(e), k = e - o * K;
         float s = 0.f;
         for (int r = 0; r < R; ++r) s = fmaf(gybuf[r * MAX_OUT + o], hin[r * LDS + k], s);
         dW[(int64_t)o * K + k] = first ? s : dW[(int64_t)o * K + k] + s;
       }
       for (int o = tid; o < d_out; o += NT) {
         float s = 0.f;
-        for (int r = 0; r < R; ++r)
-          if (G.st_order[r / T] == 0) s += gybuf[r * MAX_OUT + o];
+        for (int st = 0; st < S; ++st)   // the value streams' rows in ascending order
+          if (G.st_order[st] == 0)
+            for (int r = st * T; r < st * T + T; ++r) s += gybuf[r * MAX_OUT + o];
         db[o] = first ? s : db[o] + s;
       }
       for (int e = tid; e < R * K; e += NT) {
-        const int r = e / K, k = e - r * K;
+        const int r = fdK.div(e), k = e - r * K;
         float s = 0.f;
         for (int o = 0; o < d_out; ++o) s = fmaf(gybuf[r * MAX_OUT + o], __ldg(&Wl[(int64_t)o * K + k]), s);
         hout[r * LDS + k] = s;
@@ -616,7 +626,7 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
           float sb = 0.f;
           float sw[TDG_MAX_DIN] = {0.f, 0.f, 0.f, 0.f};
           for (int r = 0; r < R; ++r) {
-            const int s = r / T;
+            const int s = fdT.div(r);
             const int o = G.st_order[s];
             const float g = gcur[r * LDS + n];
             if (o == 0) {

@@ -72,6 +72,17 @@ struct alignas(16) DevGroup {
   DevPart parts[MAX_PARTS];
 };
 
+// e / d for 0 <= e < 2^16 and 1 <= d < 2^16 as one multiply-high by m = ceil(2^32 / d) instead of
+// a division by a runtime divisor: exact, since the error term e (m d - 2^32) / (d 2^32) stays
+// below e / 2^32 < 1 / d. d = 1 passes e through.
+struct FastDiv {
+  uint32_t m;
+  int d;
+  __device__ __forceinline__ explicit FastDiv(int d_)
+      : m(d_ > 1 ? 0xFFFFFFFFu / (uint32_t)d_ + 1u : 0u), d(d_) {}
+  __device__ __forceinline__ int div(int e) const { return d > 1 ? (int)__umulhi((uint32_t)e, m) : e; }
+};
+
 struct DevTile {
   int32_t group, row0, nvalid, seg;
   int32_t first_in_seg, problem, pad[2];   // problem: the group's parameter set
