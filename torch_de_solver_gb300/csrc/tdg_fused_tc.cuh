@@ -242,37 +242,6 @@ __device__ __forceinline__ void gemm_issue(uint32_t d, const unsigned char* a, c
   commit(bar);
 }
 
-// Split TF32: D = A . B^T as hi*hi + hi*lo + lo*hi, FP32 accumulate. A hi in shared memory (k
-// elements per row, rounded), A lo in tensor memory (columns), B streamed from global memory in
-// two K-halves of [hi | lo] blocks through opB. All threads call this (it waits on the copies and
-// the MMAs); thread 0 issues.
-__device__ void gemm3x(TcCtx& cx, uint32_t d, const unsigned char* a, uint32_t a_lo, unsigned char* opB,
-                       const unsigned char* b_src, int n, int k) {
-  const uint32_t idesc = instr_desc<false>(128, n);
-  const int kh = k / 2;
-  const uint32_t half_bytes = (uint32_t)n * kh * 4;
-  const uint32_t sbo_a = (uint32_t)(k / 4) * 128, sbo_b = (uint32_t)(kh / 4) * 128;
-  for (int h = 0; h < 2; ++h) {
-    if (h == 0) cx.ensure(opB, b_src, 2 * half_bytes);
-    else cx.load(opB, b_src + 2 * half_bytes, 2 * half_bytes);
-    if (threadIdx.x == 0) {
-      fence_after();
-      const uint32_t a0 = smem_u32(a), b0 = smem_u32(opB);
-      for (int j = 0; j < kh / 8; ++j) {
-        const int kk = h * kh + 8 * j;
-        const uint64_t ad = smem_desc(a0 + (kk / 8) * 256, 128, sbo_a);
-        const uint64_t bh = smem_desc(b0 + j * 256, 128, sbo_b);
-        const uint64_t bl = smem_desc(b0 + half_bytes + j * 256, 128, sbo_b);
-        mma<false>(d, ad, bh, idesc, h > 0 || j > 0);
-        mma<false>(d, ad, bl, idesc, true);
-        mma_ts_tf32(d, a_lo + kk, bh, idesc, true);
-      }
-      commit(cx.bar_mma);
-    }
-    cx.wait_mma();
-  }
-}
-
 // ---- jet code of the compile-time site classes (tdg_jetcls.h): rules folded into straight-line
 // code, every stream value of a (point, 4 neurons) task in registers
 template <int C>
@@ -609,20 +578,6 @@ __device__ void jet_fwd_rows(float* __restrict__ P, unsigned char* __restrict__ 
   }
 }
 
-// Split TF32: the low part x - tf32(x) of every row of P (FP32 rows), into tensor memory
-// columns [0, kp) at a_lo. Each warp writes its own lane quarter, columns split over 4 warps.
-__device__ void alo_from_rows(const float* __restrict__ P, uint32_t a_lo, int kp, uint32_t lane_addr,
-                              int lrow, int cgrp) {
-  for (int c = 8 * cgrp; c < kp; c += 8 * NCG) {
-    const float4 x0 = ld4(&P[lrow * LDS + c]), x1 = ld4(&P[lrow * LDS + c + 4]);
-    const float v[8] = {x0.x - to_tf32(x0.x), x0.y - to_tf32(x0.y), x0.z - to_tf32(x0.z),
-                        x0.w - to_tf32(x0.w), x1.x - to_tf32(x1.x), x1.y - to_tf32(x1.y),
-                        x1.z - to_tf32(x1.z), x1.w - to_tf32(x1.w)};
-    tmem_st8(a_lo + lane_addr + c, v);
-  }
-  tmem_st_wait();
-}
-
 // A operand rows into tensor memory (lane = row, column = K): hi = tf32(x) at a_hi and, for split
 // TF32, lo = x - hi at a_lo; rows >= R are zero. Each warp writes its own lane quarter.
 template <bool X3>
@@ -741,6 +696,7 @@ struct TcArgs {
 template <bool BF16, bool X3, int CM>
 __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA) {
   constexpr int ES = BF16 ? 2 : 4;
+  static_assert(!(BF16 && X3), "split TF32 is a TF32 mode");
   // TF32 and split TF32 keep every A operand in tensor memory (hi at AHI, lo at ALO), which
   // leaves both shared-memory operand buffers to the B operands; BF16 keeps A in opA
   constexpr bool TMA_A = !BF16;
@@ -934,11 +890,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), true, false, t0);
       __syncthreads();
       rows_to_tmem<X3>(P1, AHI, ALO, p16(A.width[1]), R, lane_addr, lrow, cgrp);
-    } else if (X3) {
-      jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), true, true, t0);
-      zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
-      __syncthreads();
-      alo_from_rows(P1, ALO, p16(A.width[1]), lane_addr, lrow, cgrp);
     } else {
       jet_fwd_rows<BF16, CM>(P1, opA, G, p16(A.width[1]), false, false, t0);
       zero_rows<BF16>(opA, R, p16(A.width[1]), ES);
@@ -951,8 +902,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
       const int kp = p16(K), np = p16(N);
       if constexpr (TMA_A) {
         gemm_tmem_a<X3>(cx, D1, AHI, ALO, opA, opB, wpk + TA.wfwd_off[j], np, kp, [] {});
-      } else if (X3) {
-        gemm3x(cx, D1, opA, ALO, opB, wpk + TA.wfwd_off[j], np, kp);
       } else {
         cx.ensure(opB, wpk + TA.wfwd_off[j], (uint32_t)(np * kp * ES));
         gemm_issue<BF16>(D1, opA, opB, np, kp, cx.bar_mma);
@@ -1002,11 +951,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
         jet_fwd_rows<BF16, CM>(P1, opA, G, np, true, false, tj);
         __syncthreads();
         rows_to_tmem<X3>(P1, AHI, ALO, np, R, lane_addr, lrow, cgrp);
-      } else if (X3) {
-        jet_fwd_rows<BF16, CM>(P1, opA, G, np, true, true, tj);
-        zero_rows<BF16>(opA, R, np, ES);
-        __syncthreads();
-        alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
       } else {
         jet_fwd_rows<BF16, CM>(P1, opA, G, np, false, false, tj);
         zero_rows<BF16>(opA, R, np, ES);
@@ -1284,10 +1228,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           cx.issue(opB, wpk + TA.wbwd_off[l - 1] + (uint32_t)kp * np * 4, (uint32_t)kp * np * 4);
       } else {
         zero_rows<BF16>(opA, R, np, ES);
-        if (X3) {
-          __syncthreads();
-          alo_from_rows(P1, ALO, np, lane_addr, lrow, cgrp);
-        }
         cx.publish();
       }
       // Z_l (scratch slot l-1) reached opB for the last time at the top of this layer: warps
@@ -1315,8 +1255,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           }
           ybuf[q * 128 + n] = sb;
         });
-      } else if (X3) {
-        gemm3x(cx, D1, opA, ALO, opB, wpk + TA.wbwd_off[l - 1], kp, np);
       } else {
         cx.load(opB, wpk + TA.wbwd_off[l - 1], (uint32_t)(kp * np * ES));
         gemm_issue<BF16>(D1, opA, opB, kp, np, cx.bar_mma);
@@ -1363,12 +1301,9 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
             tmem_st4(AHI + lane_addr + r, to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
           } else {
             put4<BF16>(opA, n, r, 128, make_float4(v[0], v[1], v[2], v[3]));
-            if (X3)   // lane = neuron n, columns = rows r..r+3 (the same r for the whole warp)
-              tmem_st4(ALO + lane_addr + r, v[0] - to_tf32(v[0]), v[1] - to_tf32(v[1]),
-                       v[2] - to_tf32(v[2]), v[3] - to_tf32(v[3]));
           }
         }
-        if (TMA_A || X3) tmem_st_wait();
+        if (TMA_A) tmem_st_wait();
         if (!TMA_A) red[(tid >> 7) * 128 + n] = sb;   // TMA_A: written while the dX MMAs ran
         __syncthreads();
         float* db = grad + A.b_off[l - 1];
@@ -1425,31 +1360,6 @@ __global__ void __launch_bounds__(NTC, 1) fused_tc_kernel(FusedArgs A, TcArgs TA
           }
         }
         cx.wait_mma();
-        cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
-        d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);
-      } else if (X3) {
-        // split TF32: two halves of 64 rows, [hi | lo] of H_{l-1}^T for the half in opB, then
-        // hi*hi + hi*lo + lo*hi per K-step (A lo = dL/dZ_l^T low part in tensor memory)
-        const uint32_t lo_off = (uint32_t)kp * 64 * 4;
-        const uint32_t idesc = instr_desc<false>(128, kp);
-        for (int hh = 0; hh < 2; ++hh) {
-          rows_to_opT<false, true>(P1, opB, kp, 64 * hh, 64, R, lo_off);
-          cx.publish();
-          if (tid == 0) {
-            const uint32_t a0 = smem_u32(opA), b0 = smem_u32(opB);
-            for (int j = 0; j < 8; ++j) {
-              const int kk = 64 * hh + 8 * j;
-              const uint64_t ad = smem_desc(a0 + (kk / 8) * 256, 128, 4096);
-              const uint64_t bh = smem_desc(b0 + j * 256, 128, 2048);
-              const uint64_t bl = smem_desc(b0 + lo_off + j * 256, 128, 2048);
-              mma<false>(D2, ad, bh, idesc, hh > 0 || j > 0);
-              mma<false>(D2, ad, bl, idesc, true);
-              mma_ts_tf32(D2, ALO + kk, bh, idesc, true);
-            }
-            commit(cx.bar_mma);
-          }
-          cx.wait_mma();
-        }
         cx.issue(opB, scr + (int64_t)(l - 2) * scr_slot, (uint32_t)(128 * kp * 4));   // next layer's Z
         d1_to_rows(D1, P1, kp, K, R, lane_addr, lrow, cgrp);
       } else {
