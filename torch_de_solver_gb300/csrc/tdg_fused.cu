@@ -250,31 +250,53 @@ __device__ __noinline__ void coeff_grad_warps(const DevGroup& G, const DevTerm* 
   }
 }
 
+// Thread (point p, neurons n..n+3): every per-element operation is the scalar one, in the same
+// order, applied to the four neurons (the table lookups and index arithmetic are shared by them).
+__device__ __forceinline__ float4 ld4f(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4f(float* p, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
 __device__ void jet_forward(float* __restrict__ buf, const DevGroup& G, int N) {
-  const int T = G.T;
-  const FastDiv fdN(N);
-  for (int e = threadIdx.x; e < T * N; e += NT) {
-    const int p = fdN.div(e), n = e - p * N;
+  const int T = G.T, N4 = N >> 2;   // the fused forms' widths are multiples of 4
+  const FastDiv fdN4(N4);
+  for (int e = threadIdx.x; e < T * N4; e += NT) {
+    const int p = fdN4.div(e), n = (e - p * N4) * 4;
     for (int q = 0; q < G.n_sites; ++q) {
       const int ns = G.site_nstreams[q];
       const int base = G.site_streams[q][0];
       float* zb = &buf[(base * T + p) * LDS + n];
-      const float t = tanhf(*zb);
+      const float4 z4 = ld4f(zb);
+      const float zz[4] = {z4.x, z4.y, z4.z, z4.w};
+      float t[4], s1[4], s2[4], s3[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) t[c] = tanhf(zz[c]);
       if (ns > 1) {
-        const float s1 = 1.f - t * t, s2 = -2.f * t * s1, s3 = s1 * (6.f * t * t - 2.f);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          s1[c] = 1.f - t[c] * t[c];
+          s2[c] = -2.f * t[c] * s1[c];
+          s3[c] = s1[c] * (6.f * t[c] * t[c] - 2.f);
+        }
         for (int m = ns - 1; m >= 1; --m) {
-          const int s = G.site_streams[q][m];
-          float h = 0.f;
-          for (int u = 0; u < G.st_nrule[s]; ++u) {
-            const DevRule& ru = G.rules[s][u];
-            float v = (float)ru.mult * sig_k(ru.k, t, s1, s2, s3, 0.f);
-            for (int i = 0; i < ru.k; ++i) v *= buf[(ru.sub[i] * T + p) * LDS + n];
-            h += v;
+          const int st = G.site_streams[q][m];
+          float h[4] = {0.f, 0.f, 0.f, 0.f};
+          for (int u = 0; u < G.st_nrule[st]; ++u) {
+            const DevRule& ru = G.rules[st][u];
+            float v[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) v[c] = (float)ru.mult * sig_k(ru.k, t[c], s1[c], s2[c], s3[c], 0.f);
+            for (int i = 0; i < ru.k; ++i) {
+              const float4 w = ld4f(&buf[(ru.sub[i] * T + p) * LDS + n]);
+              v[0] *= w.x; v[1] *= w.y; v[2] *= w.z; v[3] *= w.w;
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) h[c] += v[c];
           }
-          buf[(s * T + p) * LDS + n] = h;
+          st4f(&buf[(st * T + p) * LDS + n], h);
         }
       }
-      *zb = t;
+      st4f(zb, t);
     }
   }
 }
@@ -283,34 +305,54 @@ __device__ void jet_forward(float* __restrict__ buf, const DevGroup& G, int N) {
 // Streams of a site are processed from the value stream up (see DevPull).
 __device__ void jet_backward(const float* __restrict__ zbuf, float* __restrict__ gbuf,
                              const DevGroup& G, int N) {
-  const int T = G.T;
-  const FastDiv fdN(N);
-  for (int e = threadIdx.x; e < T * N; e += NT) {
-    const int p = fdN.div(e), n = e - p * N;
+  const int T = G.T, N4 = N >> 2;
+  const FastDiv fdN4(N4);
+  for (int e = threadIdx.x; e < T * N4; e += NT) {
+    const int p = fdN4.div(e), n = (e - p * N4) * 4;
     for (int q = 0; q < G.n_sites; ++q) {
       const int ns = G.site_nstreams[q];
       const int base = G.site_streams[q][0];
-      const float t = tanhf(zbuf[(base * T + p) * LDS + n]);
-      const float s1 = 1.f - t * t;
+      const float4 z4 = ld4f(&zbuf[(base * T + p) * LDS + n]);
+      const float zz[4] = {z4.x, z4.y, z4.z, z4.w};
+      float t[4], s1[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        t[c] = tanhf(zz[c]);
+        s1[c] = 1.f - t[c] * t[c];
+      }
       if (ns == 1) {
         float* g = &gbuf[(base * T + p) * LDS + n];
-        *g = *g * s1;
+        const float4 g4 = ld4f(g);
+        const float gg[4] = {g4.x * s1[0], g4.y * s1[1], g4.z * s1[2], g4.w * s1[3]};
+        st4f(g, gg);
         continue;
       }
-      const float s2 = -2.f * t * s1, s3 = s1 * (6.f * t * t - 2.f);
-      const float s4 = t * s1 * (16.f - 24.f * t * t);
+      float s2[4], s3[4], s4[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        s2[c] = -2.f * t[c] * s1[c];
+        s3[c] = s1[c] * (6.f * t[c] * t[c] - 2.f);
+        s4[c] = t[c] * s1[c] * (16.f - 24.f * t[c] * t[c]);
+      }
       for (int m = 0; m < ns; ++m) {
         const int b = G.site_streams[q][m];
-        float acc = 0.f;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
         const int pf = G.st_pull_first[b];
         for (int u = 0; u < G.st_npull[b]; ++u) {
           const DevPull& pl = G.pulls[pf + u];
-          float v = (float)pl.mult * sig_k(pl.kk, t, s1, s2, s3, s4) *
-                    gbuf[(pl.alpha * T + p) * LDS + n];
-          for (int i = 0; i < pl.n_oth; ++i) v *= zbuf[(pl.oth[i] * T + p) * LDS + n];
-          acc += v;
+          const float4 ga = ld4f(&gbuf[(pl.alpha * T + p) * LDS + n]);
+          const float gv[4] = {ga.x, ga.y, ga.z, ga.w};
+          float v[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) v[c] = (float)pl.mult * sig_k(pl.kk, t[c], s1[c], s2[c], s3[c], s4[c]) * gv[c];
+          for (int i = 0; i < pl.n_oth; ++i) {
+            const float4 w = ld4f(&zbuf[(pl.oth[i] * T + p) * LDS + n]);
+            v[0] *= w.x; v[1] *= w.y; v[2] *= w.z; v[3] *= w.w;
+          }
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[c] += v[c];
         }
-        gbuf[(b * T + p) * LDS + n] = acc;
+        st4f(&gbuf[(b * T + p) * LDS + n], acc);
       }
     }
   }
