@@ -59,14 +59,13 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
       if (n < N) {
         const float4 b = *reinterpret_cast<const float4*>(&W[n * LDS + k]);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          float v = acc[i][j];
-          v = fmaf(a[i].x, b.x, v);
-          v = fmaf(a[i].y, b.y, v);
-          v = fmaf(a[i].z, b.z, v);
-          v = fmaf(a[i].w, b.w, v);
-          acc[i][j] = v;
-        }
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].x, b.x, acc[i][j]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].y, b.y, acc[i][j]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].z, b.z, acc[i][j]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].w, b.w, acc[i][j]);
       }
     }
   }
@@ -107,14 +106,13 @@ __device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ 
         const float b0 = W[n * LDS + k], b1 = W[(n + 1) * LDS + k];
         const float b2 = W[(n + 2) * LDS + k], b3 = W[(n + 3) * LDS + k];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          float v = acc[i][j];
-          v = fmaf(a[i].x, b0, v);
-          v = fmaf(a[i].y, b1, v);
-          v = fmaf(a[i].z, b2, v);
-          v = fmaf(a[i].w, b3, v);
-          acc[i][j] = v;
-        }
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].x, b0, acc[i][j]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].y, b1, acc[i][j]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].z, b2, acc[i][j]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].w, b3, acc[i][j]);
       }
     }
   }
@@ -140,6 +138,7 @@ __device__ void gemm_dw(const float* __restrict__ Gz, const float* __restrict__ 
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+#pragma unroll 2
   for (int r = 0; r < R; ++r) {
     float ga[8], hb[8];
 #pragma unroll
