@@ -36,17 +36,21 @@ __device__ __forceinline__ float dpow_f(float x, float p) {  // d/dx x^p
   return p * powf(x, p - 1.f);
 }
 
-// Z[r][n] = sum_k H[r][k] W[n][k] (+ b[n] on value streams). 16x16 threads, 8x8 outputs each.
-__device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ W,
-                         float* __restrict__ Z, const float* __restrict__ bias,
-                         const DevGroup& G, int R, int N, int K) {
+// The three SIMT GEMMs of a tile: 16x16 threads, each with an 8x8 register tile of the 128x128
+// output. A column guard around the B loads keeps the compiler from issuing them ahead of the
+// FMAs, so every width that is a multiple of 16 runs a guard-free instantiation: JN = columns / 16
+// column groups per thread (the accumulators of the other groups are never touched), and KC = 128
+// makes the reduction length a compile-time constant for the 128-wide layers. JN = 0 is the
+// guarded form for the other widths. Every accumulator sees the same operations in the same order
+// in all forms, so the results are bitwise the same.
+
+// Z[r][n] = sum_k H[r][k] W[n][k] (+ b[n] on value streams)
+template <int JN, int KC>
+__device__ __forceinline__ void fwd_acc(const float* __restrict__ H, const float* __restrict__ W,
+                                        float (&acc)[8][8], int R, int N, int K) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  float acc[8][8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-  for (int k = 0; k < K; k += 4) {
+  const int KK = KC ? KC : K;
+  for (int k = 0; k < KK; k += 4) {
     float4 a[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -54,9 +58,9 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
       a[i] = r < R ? *reinterpret_cast<const float4*>(&H[r * LDS + k]) : make_float4(0, 0, 0, 0);
     }
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < (JN ? JN : 8); ++j) {
       const int n = tx + 16 * j;
-      if (n < N) {
+      if (JN || n < N) {
         const float4 b = *reinterpret_cast<const float4*>(&W[n * LDS + k]);
 #pragma unroll
         for (int i = 0; i < 8; ++i) acc[i][j] = fmaf(a[i].x, b.x, acc[i][j]);
@@ -69,6 +73,22 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
       }
     }
   }
+}
+
+__device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ W,
+                         float* __restrict__ Z, const float* __restrict__ bias,
+                         const DevGroup& G, int R, int N, int K) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  if (N == 128 && K == 128) fwd_acc<8, 128>(H, W, acc, R, N, K);
+  else if (N == 128) fwd_acc<8, 0>(H, W, acc, R, N, K);
+  else if (N == 64) fwd_acc<4, 0>(H, W, acc, R, N, K);
+  else if (N == 32) fwd_acc<2, 0>(H, W, acc, R, N, K);
+  else fwd_acc<0, 0>(H, W, acc, R, N, K);
   const FastDiv fdT(G.T);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -83,16 +103,13 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
   }
 }
 
-// X[r][k] = sum_n G[r][n] W[n][k]
-__device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ W,
-                        float* __restrict__ X, int R, int N, int K) {
+// X[r][k] = sum_n G[r][n] W[n][k] (JN = K / 16 column groups, NC the reduction length)
+template <int JN, int NC>
+__device__ __forceinline__ void dx_acc(const float* __restrict__ Gz, const float* __restrict__ W,
+                                       float (&acc)[8][8], int R, int N, int K) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  float acc[8][8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-  for (int n = 0; n < N; n += 4) {
+  const int NN = NC ? NC : N;
+  for (int n = 0; n < NN; n += 4) {
     float4 a[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -100,9 +117,9 @@ __device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ 
       a[i] = r < R ? *reinterpret_cast<const float4*>(&Gz[r * LDS + n]) : make_float4(0, 0, 0, 0);
     }
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < (JN ? JN : 8); ++j) {
       const int k = tx + 16 * j;
-      if (k < K) {
+      if (JN || k < K) {
         const float b0 = W[n * LDS + k], b1 = W[(n + 1) * LDS + k];
         const float b2 = W[(n + 2) * LDS + k], b3 = W[(n + 3) * LDS + k];
 #pragma unroll
@@ -116,6 +133,21 @@ __device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ 
       }
     }
   }
+}
+
+__device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ W,
+                        float* __restrict__ X, int R, int N, int K) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  if (N == 128 && K == 128) dx_acc<8, 128>(Gz, W, acc, R, N, K);
+  else if (K == 128) dx_acc<8, 0>(Gz, W, acc, R, N, K);
+  else if (K == 64) dx_acc<4, 0>(Gz, W, acc, R, N, K);
+  else if (K == 32) dx_acc<2, 0>(Gz, W, acc, R, N, K);
+  else dx_acc<0, 0>(Gz, W, acc, R, N, K);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int r = ty + 16 * i;
@@ -125,6 +157,35 @@ __device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ 
       const int k = tx + 16 * j;
       if (k < K) X[r * LDS + k] = acc[i][j];
     }
+  }
+}
+
+// dW[n][k] += sum_r G[r][n] H[r][k] over the tile's rows. Thread (ty, tx) owns n = 4 ty + 64 h
+// + (0..3) and k = 4 tx + 64 h' + (0..3) for halves h, h' < HN: HN = 1 when both widths are at
+// most 64 (the other three quarters would only multiply zeros). FREE: no bounds on the loads
+// (N = K = 64 HN; lanes past a width read rows of the 128-wide buffer that nothing stores).
+template <int HN, bool FREE>
+__device__ __forceinline__ void dw_acc(const float* __restrict__ Gz, const float* __restrict__ H,
+                                       float (&acc)[8][8], int R, int N, int K) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll 2
+  for (int r = 0; r < R; ++r) {
+    float ga[8], hb[8];
+#pragma unroll
+    for (int h = 0; h < HN; ++h) {
+      const int n = 4 * ty + 64 * h;
+      const float4 g4 = FREE || n < N ? *reinterpret_cast<const float4*>(&Gz[r * LDS + n])
+                                      : make_float4(0, 0, 0, 0);
+      ga[4 * h + 0] = g4.x; ga[4 * h + 1] = g4.y; ga[4 * h + 2] = g4.z; ga[4 * h + 3] = g4.w;
+      const int k = 4 * tx + 64 * h;
+      const float4 h4 = FREE || k < K ? *reinterpret_cast<const float4*>(&H[r * LDS + k])
+                                      : make_float4(0, 0, 0, 0);
+      hb[4 * h + 0] = h4.x; hb[4 * h + 1] = h4.y; hb[4 * h + 2] = h4.z; hb[4 * h + 3] = h4.w;
+    }
+#pragma unroll
+    for (int i = 0; i < 4 * HN; ++i)
+#pragma unroll
+      for (int j = 0; j < 4 * HN; ++j) acc[i][j] = fmaf(ga[i], hb[j], acc[i][j]);
   }
 }
 
@@ -138,25 +199,10 @@ __device__ void gemm_dw(const float* __restrict__ Gz, const float* __restrict__ 
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-#pragma unroll 2
-  for (int r = 0; r < R; ++r) {
-    float ga[8], hb[8];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int n = 4 * ty + 64 * h;
-      const float4 g4 = n < N ? *reinterpret_cast<const float4*>(&Gz[r * LDS + n])
-                              : make_float4(0, 0, 0, 0);
-      ga[4 * h + 0] = g4.x; ga[4 * h + 1] = g4.y; ga[4 * h + 2] = g4.z; ga[4 * h + 3] = g4.w;
-      const int k = 4 * tx + 64 * h;
-      const float4 h4 = k < K ? *reinterpret_cast<const float4*>(&H[r * LDS + k])
-                              : make_float4(0, 0, 0, 0);
-      hb[4 * h + 0] = h4.x; hb[4 * h + 1] = h4.y; hb[4 * h + 2] = h4.z; hb[4 * h + 3] = h4.w;
-    }
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(ga[i], hb[j], acc[i][j]);
-  }
+  if (N == 128 && K == 128) dw_acc<2, true>(Gz, H, acc, R, N, K);
+  else if (N == 64 && K == 64) dw_acc<1, true>(Gz, H, acc, R, N, K);
+  else if (N <= 64 && K <= 64) dw_acc<1, false>(Gz, H, acc, R, N, K);
+  else dw_acc<2, false>(Gz, H, acc, R, N, K);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int n = 4 * ty + 64 * (i >> 2) + (i & 3);
@@ -536,42 +582,64 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
           }
           prod *= pow_f(F, fc.power);
         }
-        outv[tm.output] += c * prod;
+        const float add = c * prod;
+#pragma unroll
+        for (int o = 0; o < MAX_OUT; ++o)   // register arrays: constant indices, unconditional
+          outv[o] += tm.output == o ? add : 0.f;   // stores (outv is never -0, so + 0 is exact)
       }
       float seed[MAX_OUT];
 #pragma unroll
       for (int o = 0; o < MAX_OUT; ++o) seed[o] = 0.f;
-      for (int o = 0; o < n_out; ++o) {
-        const float tgt = (G.target_array >= 0 && valid)
-                              ? A.arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
-        const float e = valid ? outv[o] - tgt : 0.f;
-        const float rw = (G.row_weight_array >= 0 && valid) ? A.arrays[G.row_weight_array][row0 + p] : 1.f;
+#pragma unroll
+      for (int o = 0; o < MAX_OUT; ++o) {
+        float e = 0.f, rw = 1.f, sc = 0.f;   // outputs past n_out keep zeros
+        if (o < n_out) {
+          const float tgt = (G.target_array >= 0 && valid)
+                                ? A.arrays[G.target_array][(int64_t)(row0 + p) * n_out + o] : 0.f;
+          e = valid ? outv[o] - tgt : 0.f;
+          rw = (G.row_weight_array >= 0 && valid) ? A.arrays[G.row_weight_array][row0 + p] : 1.f;
+          sc = G.seed_scale[o];
+          if (A.outputs && G.out_offset >= 0 && valid)
+            A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = outv[o];
+        }
         err2[o] = e * e * rw;
-        seed[o] = e * G.seed_scale[o] * rw;   // dL/d(out) = 2 * weight * row weight * (out - target)
-        if (A.outputs && G.out_offset >= 0 && valid)
-          A.outputs[G.out_offset + (int64_t)(row0 + p) * n_out + o] = outv[o];
+        seed[o] = e * sc * rw;   // dL/d(out) = 2 * weight * row weight * (out - target)
       }
       if (A.do_grad) {
         for (int t = 0; t < G.n_terms; ++t) {
           const DevTerm& tm = G.terms[t];
           const float c = tm.coeff_array >= 0 && valid ? A.arrays[tm.coeff_array][row0 + p] : tm.coeff;
-          const float dt = seed[tm.output] * c;
+          float so = 0.f;
+#pragma unroll
+          for (int o = 0; o < MAX_OUT; ++o) so = tm.output == o ? seed[o] : so;
+          const float dt = so * c;
           if (dt == 0.f) continue;
-          float F[MAX_TERM_FACTORS];
-          for (int f = 0; f < tm.n_factors; ++f) {
-            const DevFactor& fc = G.factors[tm.factor_first + f];
-            float v = 0.f;
-            for (int u = 0; u < fc.n_parts; ++u) {
-              const DevPart& pt = G.parts[fc.part_first + u];
-              v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
+          // the factors and their powers, each evaluated once (the same values the product
+          // rule below multiplies)
+          const int nf = tm.n_factors;
+          float F[MAX_TERM_FACTORS], PW[MAX_TERM_FACTORS];
+#pragma unroll
+          for (int f = 0; f < MAX_TERM_FACTORS; ++f) {
+            float v = 0.f, pw = 1.f;
+            if (f < nf) {
+              const DevFactor& fc = G.factors[tm.factor_first + f];
+              for (int u = 0; u < fc.n_parts; ++u) {
+                const DevPart& pt = G.parts[fc.part_first + u];
+                v = fmaf(ybuf[(pt.stream * T + p) * MAX_OUT + fc.var], pt.weight, v);
+              }
+              pw = pow_f(v, fc.power);
             }
             F[f] = v;
+            PW[f] = pw;
           }
-          for (int f = 0; f < tm.n_factors; ++f) {
+#pragma unroll
+          for (int f = 0; f < MAX_TERM_FACTORS; ++f) {
+            if (f >= nf) continue;
             const DevFactor& fc = G.factors[tm.factor_first + f];
             float d = dt * dpow_f(F[f], fc.power);
-            for (int g = 0; g < tm.n_factors; ++g)
-              if (g != f) d *= pow_f(F[g], G.factors[tm.factor_first + g].power);
+#pragma unroll
+            for (int g = 0; g < MAX_TERM_FACTORS; ++g)
+              if (g < nf && g != f) d *= PW[g];   // (a multiplication by 1 would not change d)
             for (int u = 0; u < fc.n_parts; ++u) {
               const DevPart& pt = G.parts[fc.part_first + u];
               gybuf[(pt.stream * T + p) * MAX_OUT + fc.var] += d * pt.weight;
@@ -583,7 +651,9 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     // deterministic FP64 reduction of squared errors: warp shuffle, then warps in order
     {
       const int lane = tid & 31, warp = tid >> 5;
-      for (int o = 0; o < n_out; ++o) {
+#pragma unroll
+      for (int o = 0; o < MAX_OUT; ++o) {
+        if (o >= n_out) continue;
         double v = (double)err2[o];
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
@@ -672,14 +742,18 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
             const float g = gcur[r * LDS + n];
             if (o == 0) {
               sb += g;
-              for (int a = 0; a < d_in; ++a) sw[a] = fmaf(g, xsbuf[r * TDG_MAX_DIN + a], sw[a]);
+#pragma unroll
+              for (int a = 0; a < TDG_MAX_DIN; ++a)
+                if (a < d_in) sw[a] = fmaf(g, xsbuf[r * TDG_MAX_DIN + a], sw[a]);
             } else if (o == 1) {
               const int ax = G.st_axis[s];
-              for (int a = 0; a < d_in; ++a) if (a == ax) sw[a] += g;
+#pragma unroll
+              for (int a = 0; a < TDG_MAX_DIN; ++a) if (a == ax) sw[a] += g;
             }
           }
-          for (int a = 0; a < d_in; ++a)
-            dW0[n * d_in + a] = first ? sw[a] : dW0[n * d_in + a] + sw[a];
+#pragma unroll
+          for (int a = 0; a < TDG_MAX_DIN; ++a)
+            if (a < d_in) dW0[n * d_in + a] = first ? sw[a] : dW0[n * d_in + a] + sw[a];
           db0[n] = first ? sb : db0[n] + sb;
         }
       }
