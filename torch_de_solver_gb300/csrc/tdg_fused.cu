@@ -90,6 +90,9 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
   else if (N == 32) fwd_acc<2, 0>(H, W, acc, R, N, K);
   else fwd_acc<0, 0>(H, W, acc, R, N, K);
   const FastDiv fdT(G.T);
+  float bj[8];   // this thread's 8 biases, loaded once
+#pragma unroll
+  for (int j = 0; j < 8; ++j) bj[j] = tx + 16 * j < N ? __ldg(&bias[tx + 16 * j]) : 0.f;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int r = ty + 16 * i;
@@ -98,7 +101,7 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int n = tx + 16 * j;
-      if (n < N) Z[r * LDS + n] = acc[i][j] + (val ? __ldg(&bias[n]) : 0.f);
+      if (n < N) Z[r * LDS + n] = acc[i][j] + (val ? bj[j] : 0.f);
     }
   }
 }
@@ -168,7 +171,7 @@ template <int HN, bool FREE>
 __device__ __forceinline__ void dw_acc(const float* __restrict__ Gz, const float* __restrict__ H,
                                        float (&acc)[8][8], int R, int N, int K) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll 2
+#pragma unroll 4
   for (int r = 0; r < R; ++r) {
     float ga[8], hb[8];
 #pragma unroll
@@ -211,13 +214,14 @@ __device__ void gemm_dw(const float* __restrict__ Gz, const float* __restrict__ 
     for (int h = 0; h < 2; ++h) {
       const int k = 4 * tx + 64 * h;
       if (k >= K) continue;
-      float4* dst = reinterpret_cast<float4*>(&dW[(int64_t)n * K + k]);
-      float4 v = make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
-      if (!first) {
-        const float4 o = *dst;
-        v.x += o.x; v.y += o.y; v.z += o.z; v.w += o.w;
-      }
-      *dst = v;
+      // the segment's first tile stores, the later ones add without waiting for a load (one
+      // thread owns each address, so the adds keep their order)
+      float* dst = &dW[(int64_t)n * K + k];
+      if (first)
+        *reinterpret_cast<float4*>(dst) =
+            make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
+      else
+        red_add4(dst, acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
     }
   }
   // bias gradient: one thread per neuron, the value streams' rows in ascending order
@@ -227,7 +231,8 @@ __device__ void gemm_dw(const float* __restrict__ Gz, const float* __restrict__ 
     for (int st = 0; st * T < R; ++st)
       if (G.st_order[st] == 0)
         for (int r = st * T; r < st * T + T && r < R; ++r) s += Gz[r * LDS + n];
-    db[n] = first ? s : db[n] + s;
+    if (first) db[n] = s;
+    else red_add1(&db[n], s);
   }
 }
 
@@ -403,17 +408,28 @@ __device__ void jet_backward(const float* __restrict__ zbuf, float* __restrict__
   }
 }
 
-// Stage W [N x K] into shared memory. Vector loads need a 16-byte aligned W; the weights of
+// 16-byte asynchronous copies global -> shared (cp.async, L2 only): a stage is issued ahead and
+// lands while other work runs; cp.async.wait_group then the next barrier make it visible.
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+               :: "r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" :: "n"(PENDING) : "memory");
+}
+
+// Stage W [N x K] into shared memory, asynchronously when W is 16-byte aligned; the weights of
 // problem p start at p * n_params floats, which is not a multiple of 4 for odd parameter counts,
-// so misaligned layers are read element by element.
+// so misaligned layers are read element by element (synchronously). Commits one copy group.
 __device__ void load_weights(float* __restrict__ wbuf, const float* __restrict__ W, int N, int K) {
   if ((reinterpret_cast<uintptr_t>(W) & 15) == 0) {
     const int K4 = K >> 2;
     const FastDiv fdK4(K4);
     for (int e = threadIdx.x; e < N * K4; e += NT) {
       const int n = fdK4.div(e), k = (e - n * K4) * 4;
-      *reinterpret_cast<float4*>(&wbuf[n * LDS + k]) =
-          __ldg(reinterpret_cast<const float4*>(&W[(int64_t)n * K + k]));
+      cp_async16(&wbuf[n * LDS + k], &W[(int64_t)n * K + k]);
     }
   } else {
     const FastDiv fdK(K);
@@ -422,8 +438,22 @@ __device__ void load_weights(float* __restrict__ wbuf, const float* __restrict__
       wbuf[n * LDS + k] = __ldg(&W[(int64_t)n * K + k]);
     }
   }
+  cp_async_commit();
 }
 
+// rows [R x K] of a saved layer (global scratch, row stride LDS) into shared memory,
+// asynchronously; commits one copy group
+__device__ void fetch_rows(float* __restrict__ dst, const float* __restrict__ src, int R, int K) {
+  const int K4 = K >> 2;
+  const FastDiv fdK4(K4);
+  for (int e = threadIdx.x; e < R * K4; e += NT) {
+    const int r = fdK4.div(e), k = (e - r * K4) * 4;
+    cp_async16(&dst[r * LDS + k], &src[r * LDS + k]);
+  }
+  cp_async_commit();
+}
+
+// rows [R x K] of shared memory into the global scratch (row stride LDS)
 __device__ void copy_rows(float* __restrict__ dst, const float* __restrict__ src, int R, int K) {
   const int K4 = K >> 2;
   const FastDiv fdK4(K4);
@@ -479,6 +509,9 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     const FastDiv fdT(T);
     const int nvalid = tile.nvalid, row0 = tile.row0;
     const float* prm = A.params + (int64_t)G.problem * A.n_params;
+    // the first hidden GEMM's weights land during the coordinates, the input layer and its jets
+    // (the weight buffer's last reader, the previous tile's last GEMM, ended at a barrier)
+    if (L > 2) load_weights(wbuf, prm + A.w_off[1], A.width[2], A.width[1]);
 
     // ---- coordinates of every row (site point + FP32 offset), zero for padding points
     for (int e = tid; e < R * d_in; e += NT) {
@@ -524,10 +557,12 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     // ---- hidden layers
     for (int l = 1; l < L - 1; ++l) {
       const int K = A.width[l], N = A.width[l + 1];
-      load_weights(wbuf, prm + A.w_off[l], N, K);
+      cp_async_wait<0>();   // W_l, issued after the previous GEMM
       __syncthreads();
       gemm_fwd(hin, wbuf, hout, prm + A.b_off[l], G, R, N, K);
       __syncthreads();
+      if (l + 1 < L - 1)    // the next layer's weights land during this layer's jets
+        load_weights(wbuf, prm + A.w_off[l + 1], A.width[l + 2], N);
       if (A.do_grad) copy_rows(scr + (int64_t)l * RMAX * LDS, hout, R, N);
       jet_forward(hout, G, N);
       __syncthreads();
@@ -678,7 +713,8 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
       float s = 0.f;
       for (int w = 0; w < NT / 32; ++w) s += cred[w * TDG_MAX_COEFF + tid];
       float* dst = grad + A.coeff_off + tid;
-      *dst = first ? s : *dst + s;
+      if (first) *dst = s;
+      else red_add1(dst, s);
     }
     // output layer: dW, db, and dL/dH of the last hidden layer into hout
     {
@@ -691,14 +727,16 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
         const int o = fdK.div(e), k = e - o * K;
         float s = 0.f;
         for (int r = 0; r < R; ++r) s = fmaf(gybuf[r * MAX_OUT + o], hin[r * LDS + k], s);
-        dW[(int64_t)o * K + k] = first ? s : dW[(int64_t)o * K + k] + s;
+        if (first) dW[(int64_t)o * K + k] = s;
+        else red_add1(&dW[(int64_t)o * K + k], s);
       }
       for (int o = tid; o < d_out; o += NT) {
         float s = 0.f;
         for (int st = 0; st < S; ++st)   // the value streams' rows in ascending order
           if (G.st_order[st] == 0)
             for (int r = st * T; r < st * T + T; ++r) s += gybuf[r * MAX_OUT + o];
-        db[o] = first ? s : db[o] + s;
+        if (first) db[o] = s;
+        else red_add1(&db[o], s);
       }
       for (int e = tid; e < R * K; e += NT) {
         const int r = fdK.div(e), k = e - r * K;
@@ -713,14 +751,20 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
     for (int l = L - 1; l >= 1; --l) {
       // layer l: H_l = jet(Z_l), Z_l = Linear_{l-1}(H_{l-1}); width[l] neurons
       const int N = A.width[l];
-      copy_rows(other, scr + (int64_t)(l - 1) * RMAX * LDS, R, N);
+      fetch_rows(other, scr + (int64_t)(l - 1) * RMAX * LDS, R, N);
+      if (l >= 2) {   // W_{l-1} lands during the jet adjoint (the weight buffer is free)
+        load_weights(wbuf, prm + A.w_off[l - 1], N, A.width[l - 1]);
+        cp_async_wait<1>();   // Z_l
+      } else {
+        cp_async_wait<0>();
+      }
       __syncthreads();
       jet_backward(other, gcur, G, N);   // gcur: dL/dZ_l
       __syncthreads();
       if (l >= 2) {
         const int K = A.width[l - 1];
-        copy_rows(other, scr + (int64_t)(l - 2) * RMAX * LDS, R, K);
-        load_weights(wbuf, prm + A.w_off[l - 1], N, K);
+        fetch_rows(other, scr + (int64_t)(l - 2) * RMAX * LDS, R, K);
+        cp_async_wait<0>();   // Z_{l-1} and W_{l-1}
         __syncthreads();
         jet_forward(other, G, K);          // other: H_{l-1}
         __syncthreads();
@@ -736,25 +780,31 @@ __global__ void __launch_bounds__(NT, 1) fused_fp32_kernel(FusedArgs A) {
         for (int n = tid; n < N; n += NT) {
           float sb = 0.f;
           float sw[TDG_MAX_DIN] = {0.f, 0.f, 0.f, 0.f};
+          // branch-free and unrolled, so that the rows' loads overlap: a value row adds g to the
+          // bias and g x_a to column a, a first-derivative row along a adds g to column a (adding
+          // zero elsewhere leaves every sum as the per-kind branches would)
+#pragma unroll 4
           for (int r = 0; r < R; ++r) {
             const int s = fdT.div(r);
             const int o = G.st_order[s];
+            const int ax = o == 1 ? G.st_axis[s] : -1;
             const float g = gcur[r * LDS + n];
-            if (o == 0) {
-              sb += g;
+            const float gv = o == 0 ? g : 0.f;
+            const float4 xv = *reinterpret_cast<const float4*>(&xsbuf[r * TDG_MAX_DIN]);
+            const float xa[TDG_MAX_DIN] = {xv.x, xv.y, xv.z, xv.w};
+            sb += gv;
 #pragma unroll
-              for (int a = 0; a < TDG_MAX_DIN; ++a)
-                if (a < d_in) sw[a] = fmaf(g, xsbuf[r * TDG_MAX_DIN + a], sw[a]);
-            } else if (o == 1) {
-              const int ax = G.st_axis[s];
-#pragma unroll
-              for (int a = 0; a < TDG_MAX_DIN; ++a) if (a == ax) sw[a] += g;
-            }
+            for (int a = 0; a < TDG_MAX_DIN; ++a)
+              if (a < d_in) sw[a] = fmaf(gv, xa[a], sw[a]) + (a == ax ? g : 0.f);
           }
 #pragma unroll
           for (int a = 0; a < TDG_MAX_DIN; ++a)
-            if (a < d_in) dW0[n * d_in + a] = first ? sw[a] : dW0[n * d_in + a] + sw[a];
-          db0[n] = first ? sb : db0[n] + sb;
+            if (a < d_in) {
+              if (first) dW0[n * d_in + a] = sw[a];
+              else red_add1(&dW0[n * d_in + a], sw[a]);
+            }
+          if (first) db0[n] = sb;
+          else red_add1(&db0[n], sb);
         }
       }
     }

@@ -83,6 +83,17 @@ struct FastDiv {
   __device__ __forceinline__ int div(int e) const { return d > 1 ? (int)__umulhi((uint32_t)e, m) : e; }
 };
 
+// fire-and-forget add of one float to global memory
+__device__ __forceinline__ void red_add1(float* dst, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" :: "l"(dst), "f"(v) : "memory");
+}
+
+// fire-and-forget vector add of 4 floats to global memory (16-byte aligned)
+__device__ __forceinline__ void red_add4(float* dst, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
+               :: "l"(dst), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+
 struct DevTile {
   int32_t group, row0, nvalid, seg;
   int32_t first_in_seg, problem, pad[2];   // problem: the group's parameter set

@@ -161,17 +161,6 @@ __device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
 }
 
-// fire-and-forget add of one float to global memory
-__device__ __forceinline__ void red_add1(float* dst, float v) {
-  asm volatile("red.global.add.f32 [%0], %1;" :: "l"(dst), "f"(v) : "memory");
-}
-
-// fire-and-forget vector add of 4 floats to global memory (16-byte aligned)
-__device__ __forceinline__ void red_add4(float* dst, float a, float b, float c, float d) {
-  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
-               :: "l"(dst), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
-}
-
 __device__ __forceinline__ float to_tf32(float x) {
   // round to the nearest TF32 value (10 explicit mantissa bits), ties away from zero: add half a
   // TF32 unit in the last place to the magnitude bits, then clear the 13 low mantissa bits
