@@ -24,6 +24,8 @@ def units():
     out = [(f'tdg_tc_inst.cu', f'tdg_tc_{p}_c{c}.o',
             [f'-DTDG_TC_PREC={p}', f'-DTDG_TC_BF16={b}', f'-DTDG_TC_X3={x}', f'-DTDG_TC_CLS={c}'])
            for p, b, x in TC_PRECISIONS for c in range(TC_CLASSES)]
+    # the FP32 fused kernel: one object per main site class, from tdg_fp32_inst.cu
+    out += [('tdg_fp32_inst.cu', f'tdg_fp32_c{c}.o', [f'-DTDG_F32_CLS={c}']) for c in range(TC_CLASSES)]
     return out + [(src, src.replace('.cu', '.o'), []) for src in SOURCES]
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 LIB = os.path.join(PKG, 'libtdg.so')

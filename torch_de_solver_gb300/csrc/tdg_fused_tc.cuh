@@ -2,7 +2,7 @@
 // Each (precision, main site class) variant is instantiated in its own object, compiled from
 // tdg_tc_inst.cu with the variant's -D flags, so that all of them compile in parallel.
 //
-// Same computation as fused_fp32_kernel (tdg_fused.cu): one persistent CTA per SM walks tiles of
+// Same computation as fused_fp32_kernel (tdg_fused_fp32.cuh): one persistent CTA per SM walks tiles of
 // 128 (stream, point) rows through the tanh-jet forward, the operator program and loss, and the
 // hand-written adjoint. Every hidden-layer GEMM runs on the tensor cores:
 //   forward  Z_{j+1}[rows x N]  = H_j[rows x K] . W_j^T          (A = H, B = W packed K-major)
@@ -18,6 +18,7 @@
 #include <utility>
 #include "tdg_internal.h"
 #include "tdg_jetcls.h"
+#include "tdg_jetcode.cuh"
 #include "tdg_tc.cuh"
 
 namespace tdg {
@@ -96,40 +97,6 @@ __device__ __noinline__ void coeff_grad_tile(const DevGroup& G, const DevTerm* _
   }
 }
 
-__device__ __forceinline__ float4 f4mul(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
-__device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-__device__ __forceinline__ float4 f4scale(float4 a, float c) { return make_float4(a.x * c, a.y * c, a.z * c, a.w * c); }
-
-struct Sig {   // tanh and its derivatives, as functions of t = tanh(z), for 4 neurons
-  float4 t, s1, s2, s3, s4;
-  __device__ __forceinline__ void make(const float4 z, bool need4) {
-    from_t(make_float4(tanhf(z.x), tanhf(z.y), tanhf(z.z), tanhf(z.w)), need4);
-  }
-  // from t = tanh(z) saved by the forward pass
-  __device__ __forceinline__ void from_t(const float4 tv, bool need4) {
-    t = tv;
-    const float4 tt = f4mul(t, t);
-    s1 = make_float4(1.f - tt.x, 1.f - tt.y, 1.f - tt.z, 1.f - tt.w);
-    s2 = f4scale(f4mul(t, s1), -2.f);
-    s3 = f4mul(s1, make_float4(6.f * tt.x - 2.f, 6.f * tt.y - 2.f, 6.f * tt.z - 2.f, 6.f * tt.w - 2.f));
-    s4 = need4 ? f4mul(f4mul(t, s1), make_float4(16.f - 24.f * tt.x, 16.f - 24.f * tt.y,
-                                                  16.f - 24.f * tt.z, 16.f - 24.f * tt.w))
-               : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  // the k-th derivative; k is the same for every thread of a group's table entry (uniform branch)
-  __device__ __forceinline__ float4 sel(int k) const {
-    switch (k) {
-      case 0: return t;
-      case 1: return s1;
-      case 2: return s2;
-      case 3: return s3;
-      default: return s4;
-    }
-  }
-};
-
-__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
-__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float4 ld4o(const unsigned char* b, uint32_t off) {
   return *reinterpret_cast<const float4*>(b + off);
 }
@@ -242,29 +209,7 @@ __device__ __forceinline__ void gemm_issue(uint32_t d, const unsigned char* a, c
   commit(bar);
 }
 
-// ---- jet code of the compile-time site classes (tdg_jetcls.h): rules folded into straight-line
-// code, every stream value of a (point, 4 neurons) task in registers
-template <int C>
-__host__ __device__ constexpr jetcls::Rules rules_of() { return jetcls::make_rules(jetcls::kSiteClasses[C]); }
-
-template <typename F, int... I>
-__device__ __forceinline__ void sfor_(F& f, std::integer_sequence<int, I...>) {
-  (f(std::integral_constant<int, I>{}), ...);
-}
-template <int N, typename F>
-__device__ __forceinline__ void sfor(F&& f) { sfor_(f, std::make_integer_sequence<int, N>{}); }
-
-// run f(integral_constant<C>) for the site class `cls` when it is one this kernel carries: the
-// value-only class 0 and the plan's main class CM (each kernel instantiation carries two, which
-// keeps its code small); false otherwise (the table-driven code runs)
-template <int CM, typename F>
-__device__ __forceinline__ bool with_class(int cls, F&& f) {
-  if (cls == 0) return f(std::integral_constant<int, 0>{});
-  if constexpr (CM > 0) {
-    if (cls == CM) return f(std::integral_constant<int, CM>{});
-  }
-  return false;
-}
+// ---- jet code of the compile-time site classes: the helpers are in tdg_jetcode.cuh
 
 // f(T) with the points per tile T a compile-time constant when the group is a single site of
 // class C (then T = 128 / streams); for the value-only class also f(runtime T) for other groups.
@@ -281,20 +226,6 @@ __device__ __forceinline__ bool with_tile_points(const DevGroup& G, F&& f) {
     return true;
   }
   return false;
-}
-
-// H_M = sum_u mult * tanh^(k)(z_0) * prod Z[sub]  (same operation order as the table rules)
-template <int C, int M, int NS>
-__device__ __forceinline__ float4 cls_rule_sum(const Sig& sg, const float4 (&z)[NS]) {
-  float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
-  sfor<rules_of<C>().nrule[M]>([&](auto uc) {
-    constexpr int U = decltype(uc)::value;
-    constexpr int K = rules_of<C>().k[M][U];
-    float4 v = f4scale(sg.sel(K), (float)rules_of<C>().mult[M][U]);
-    sfor<K>([&](auto fc) { v = f4mul(v, z[rules_of<C>().sub[M][U][decltype(fc)::value]]); });
-    h = f4add(h, v);
-  });
-  return h;
 }
 
 // forward jet of one site for (point p, neurons n..n+3): plain Z rows of P -> H rows (in place

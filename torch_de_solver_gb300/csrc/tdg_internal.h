@@ -129,7 +129,8 @@ constexpr size_t fused_smem_bytes() {
          + sizeof(float) * (NT / 32) * TDG_MAX_COEFF + 64;
 }
 
-cudaError_t launch_fused_fp32(const FusedArgs& a, int n_ctas, cudaStream_t s);
+// the FP32 fused kernel, variant of the main site class cls_main (tdg_fp32_inst.cu)
+cudaError_t launch_fused_fp32(const FusedArgs& a, int cls_main, int n_ctas, cudaStream_t s);
 
 // tensor-core path: packed hidden weights (per problem p and hidden Linear j: W_j as an np x kp
 // K-major operand at p * wpack_stride + fwd_off[j] and W_j^T as kp x np at p * wpack_stride +
@@ -193,6 +194,10 @@ cudaError_t launch_fused_tc(const FusedArgs& a, const TcLaunch& t, int n_ctas, c
 TDG_TC_EACH_CLASS(TDG_TC_DECLARE, tf32)
 TDG_TC_EACH_CLASS(TDG_TC_DECLARE, bf16)
 TDG_TC_EACH_CLASS(TDG_TC_DECLARE, 3x)
+#define TDG_F32_FN_(C) launch_fp32_c##C
+#define TDG_F32_FN(C) TDG_F32_FN_(C)
+#define TDG_F32_DECLARE(P, C) cudaError_t TDG_F32_FN(C)(const FusedArgs& a, int n_ctas, cudaStream_t s);
+TDG_TC_EACH_CLASS(TDG_F32_DECLARE, fp32)
 cudaError_t launch_bounded_wait_selftest(int max_polls, int* gave_up, cudaStream_t s);
 cudaError_t launch_reduce_grad(const float* partial, int64_t part_stride, const int32_t* seg_begin,
                                const int32_t* seg_list, int n_problems, int64_t n_params,

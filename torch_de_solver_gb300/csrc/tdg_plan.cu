@@ -59,7 +59,7 @@ struct tdg_plan {
   int n_coeff = 0;
   int n_problems = 0, n_slots = 0, n_tiles = 0, n_ctas = 0, n_segments = 0, max_streams = 0;
   int precision = 0, form = 0;
-  int cls_main = 0;   // the tensor-core kernel variant: the site class with the most rows
+  int cls_main = 0;   // the fused kernels' variant: the site class with the most rows
   double flops_hidden = 0, flops_total = 0;
   std::vector<const float*> arrays;
   std::vector<int64_t> array_len;
@@ -482,8 +482,8 @@ tdg_status tdg_plan_create_scheduled(const tdg_problem_desc* desc, const tdg_sch
     p->flops_hidden += 3.0 * 2.0 * (double)g.n_rows * S * hidden_pairs;
     p->flops_total += 3.0 * 2.0 * (double)g.n_rows * S * all_pairs;
   }
-  // the tensor-core kernel variant: besides the value-only class, it carries the compile-time
-  // jets of one site class, the one covering the most rows (other sites run the tables)
+  // the fused kernels' variant: besides the value-only class, it carries the compile-time jets
+  // of one site class, the one covering the most rows (other sites run the tables)
   {
     std::vector<int64_t> rows_of_class(jetcls::N_CLASSES, 0);
     for (int gi = 0; gi < d.n_groups; ++gi)
@@ -696,7 +696,7 @@ static tdg_status run(tdg_plan* p, const float* params, float* grad, double* los
     return TDG_OK;
   }
   if (p->precision == TDG_PREC_FP32) {
-    e = launch_fused_fp32(a, p->n_ctas, s);
+    e = launch_fused_fp32(a, p->cls_main, p->n_ctas, s);
   } else {
     TcLaunch t{};
     t.bf16 = p->precision == TDG_PREC_BF16;
