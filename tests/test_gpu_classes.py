@@ -1,7 +1,7 @@
 """Every compile-time jet class on the GPU: one small autograd problem per class whose residual site
-has that layout, so the tensor-core kernel variant of that class runs. Loss and gradient against
-the oracle in FP64 (relative 1e-5, FP32 tolerance) for the split-TF32 and FP32 paths, and the
-compiled jets against the table-driven jets of the same build (relative 1e-6)."""
+has that layout, so the tensor-core and FP32 kernel variants of that class run. Loss and gradient
+against the oracle in FP64 (relative 1e-5, FP32 tolerance) for the split-TF32 and FP32 paths, and
+the compiled jets against the table-driven jets of the same build (relative 1e-6) for both."""
 import numpy as np
 import pytest
 import torch
@@ -41,3 +41,5 @@ def test_class_against_oracle_and_tables(name, monkeypatch):
     monkeypatch.setenv('TDG_JET_TABLES', '1')
     lt, gt, _ = _loss_grad(T, builder, '3xtf32')
     assert rel(l3, lt) < 1e-6 and rel(g3, gt) < 1e-6
+    lt1, gt1, _ = _loss_grad(T, builder, 'fp32')
+    assert rel(l1, lt1) < 1e-6 and rel(g1, gt1) < 1e-6
