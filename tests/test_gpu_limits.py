@@ -63,6 +63,31 @@ def test_any_width_runs_in_the_plain_form(widths):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize('precision', ['fp32', '3xtf32'])
+def test_one_hidden_layer_runs_fused(precision):
+    """A network with a single hidden layer has no hidden GEMM: the fused kernels go from the
+    input layer's jets straight to the output layer (no weights staged for a GEMM). Loss and
+    gradient against the FP64 oracle, and a few training steps."""
+    import torch_de_solver_gb300 as T
+    b = lambda api, dtype='float32': cases.burgers_ag(api, n=16, dtype=dtype, widths=(2, 32, 1))
+    prob, onet = O.build_problem(b, 'float64')
+    l_ref, ln_ref, g_ref, _ = O.loss_and_grad(prob, onet)
+    m = _compile(T, b, precision=precision)
+    assert m.solution_cls.form == 'fused'
+    w = torch.nn.utils.parameters_to_vector(onet.parameters()).detach().float()
+    torch.nn.utils.vector_to_parameters(w.to(m.solution_cls.device), m.net.parameters())
+    loss, lossn = m.solution_cls.evaluate()
+    loss.backward()
+    grad = torch.cat([p.grad.reshape(-1) for p in m.net.parameters()]).double().cpu().numpy()
+    assert rel(loss.item(), l_ref) < 1e-5 and rel(lossn.item(), ln_ref) < 1e-5
+    assert rel(grad, g_ref.numpy()) < 1e-5, rel(grad, g_ref.numpy())
+    first = loss.item()
+    m.train(T.Optimizer('Adam', {'lr': 1e-3}), 21)
+    m.solution_cls.check_status()
+    assert m.solution_cls.evaluate(save_graph=False)[0].item() < first
+
+
+@pytest.mark.gpu
 def test_unsupported_networks_are_refused():
     import torch_de_solver_gb300 as T
     d, bc, eq, net, kw = cases.burgers_ag(T, n=8)
