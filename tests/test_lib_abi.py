@@ -82,3 +82,19 @@ def test_schedule_is_validated_before_the_description():
         assert lib.tdg_plan_create_scheduled(ctypes.byref(desc), ctypes.byref(sc),
                                              ctypes.byref(h)) == _lib.ERR_INVALID, bad
         assert b'schedule' in lib.tdg_last_error()
+
+
+def test_build_compiles_both_fused_kernels_once_per_site_class():
+    """The build recipe instantiates the tensor-core kernel per (precision, site class) and the
+    FP32 kernel per site class, for every class of tdg_jetcls.h (the dispatch tables of both
+    kernels index them by class)."""
+    from torch_de_solver_gb300.csrc import build
+    src = open(os.path.join(ROOT, 'torch_de_solver_gb300', 'csrc', 'tdg_jetcls.h')).read()
+    n_classes = int(re.search(r'constexpr int N_CLASSES = (\d+);', src).group(1))
+    assert build.TC_CLASSES == n_classes
+    objs = {obj for _, obj, _ in build.units()}
+    for c in range(n_classes):
+        assert f'tdg_fp32_c{c}.o' in objs
+        for prec, _, _ in build.TC_PRECISIONS:
+            assert f'tdg_tc_{prec}_c{c}.o' in objs
+    assert len(objs) == len(build.units())   # no object built twice
