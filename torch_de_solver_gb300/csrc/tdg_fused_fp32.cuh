@@ -106,7 +106,7 @@ __device__ void gemm_fwd(const float* __restrict__ H, const float* __restrict__ 
   }
 }
 
-// X[r][k] = sum_n G[r][n] W[n][k] (JN = K / 16 column groups, NC the reduction length)
+// X[r][k] = sum_n G[r][n] W[n][k] (JN = K / 16 column groups of stride 16, NC the reduction length)
 template <int JN, int NC>
 __device__ __forceinline__ void dx_acc(const float* __restrict__ Gz, const float* __restrict__ W,
                                        float (&acc)[8][8], int R, int N, int K) {
@@ -138,6 +138,45 @@ __device__ __forceinline__ void dx_acc(const float* __restrict__ Gz, const float
   }
 }
 
+// The same for K = 64 HN with 4 contiguous columns per half: thread (ty, tx) owns k = 4 tx +
+// 64 h + (0..3), so each row of W is read as 16-byte vectors (HN vectors per n instead of 4 HN
+// scalar loads); the accumulators see the same FMAs in the same order.
+template <int HN, int NC>
+__device__ __forceinline__ void dx_acc4(const float* __restrict__ Gz, const float* __restrict__ W,
+                                        float (&acc)[8][8], int R, int N) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int NN = NC ? NC : N;
+  for (int n = 0; n < NN; n += 4) {
+    float4 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = ty + 16 * i;
+      a[i] = r < R ? *reinterpret_cast<const float4*>(&Gz[r * LDS + n]) : make_float4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int h = 0; h < HN; ++h) {
+      const int k = 4 * tx + 64 * h;
+      const float4 b0 = *reinterpret_cast<const float4*>(&W[n * LDS + k]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&W[(n + 1) * LDS + k]);
+      const float4 b2 = *reinterpret_cast<const float4*>(&W[(n + 2) * LDS + k]);
+      const float4 b3 = *reinterpret_cast<const float4*>(&W[(n + 3) * LDS + k]);
+      const float bx[4][4] = {{b0.x, b1.x, b2.x, b3.x}, {b0.y, b1.y, b2.y, b3.y},
+                              {b0.z, b1.z, b2.z, b3.z}, {b0.w, b1.w, b2.w, b3.w}};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][4 * h + c] = fmaf(a[i].x, bx[c][0], acc[i][4 * h + c]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][4 * h + c] = fmaf(a[i].y, bx[c][1], acc[i][4 * h + c]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][4 * h + c] = fmaf(a[i].z, bx[c][2], acc[i][4 * h + c]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i][4 * h + c] = fmaf(a[i].w, bx[c][3], acc[i][4 * h + c]);
+      }
+    }
+  }
+}
+
 __device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ W,
                         float* __restrict__ X, int R, int N, int K) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -146,10 +185,25 @@ __device__ void gemm_dx(const float* __restrict__ Gz, const float* __restrict__ 
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-  if (N == 128 && K == 128) dx_acc<8, 128>(Gz, W, acc, R, N, K);
-  else if (K == 128) dx_acc<8, 0>(Gz, W, acc, R, N, K);
-  else if (K == 64) dx_acc<4, 0>(Gz, W, acc, R, N, K);
-  else if (K == 32) dx_acc<2, 0>(Gz, W, acc, R, N, K);
+  if (K == 128 || K == 64) {   // 4 contiguous columns per half
+    if (N == 128 && K == 128) dx_acc4<2, 128>(Gz, W, acc, R, N);
+    else if (K == 128) dx_acc4<2, 0>(Gz, W, acc, R, N);
+    else dx_acc4<1, 0>(Gz, W, acc, R, N);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = ty + 16 * i;
+      if (r >= R) continue;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = 4 * tx + 64 * h;
+        if (k < K)
+          *reinterpret_cast<float4*>(&X[r * LDS + k]) =
+              make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
+      }
+    }
+    return;
+  }
+  if (K == 32) dx_acc<2, 0>(Gz, W, acc, R, N, K);
   else dx_acc<0, 0>(Gz, W, acc, R, N, K);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
